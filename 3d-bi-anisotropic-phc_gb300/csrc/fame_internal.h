@@ -1,0 +1,98 @@
+// Internal plan object and kernel launchers of the FAME GB300 library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/fame.h"
+#include "fame_types.cuh"
+
+namespace fame {
+
+// Which vectors of a batch belong to which k-point instance, and which are
+// still active (converged vectors of a batched solve are skipped).
+struct VecCtx {
+  const int* inst = nullptr;    // device [nvec] instance index, or null: v % nk
+  const int* active = nullptr;  // device [nvec] 0/1, or null: all active
+  int nk = 1;
+};
+
+FAME_HD int vec_inst(const VecCtx& c, int v) { return c.inst ? c.inst[v] : (v % c.nk); }
+
+// Device-side data of one precision.
+template <class R> struct PlanData {
+  cx<R>* lam = nullptr;  // [nk][3n]  lambda_x | lambda_y | lambda_z  (QP symbols, delta = 1/n)
+  cx<R>* tau = nullptr;  // [nk][3]   exp(i*theta_d/n): Bloch phase of one periodic shift
+  cx<R>* sxyz = nullptr; // [nk][3n]  S_sDFT per axis (the MtxVecMul_FFT phase)
+  cx<R>* mat = nullptr;  // [nk][nphase][27]: Herm(N) | Herm(M) | J, row-major 3x3 each
+};
+
+struct Plan {
+  int n = 0;         // cubic grid n1 = n2 = n3 = n
+  long long Nq = 0;  // n^3
+  int nk = 0;        // k-point instances
+  int nphase = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<double> theta;          // [nk][3]
+  std::vector<double> mat_host;       // [nk][nphase][27][2] covariant N | M | J blocks
+  uint8_t* d_phase = nullptr;         // [Nq] phase id per vertex
+  PlanData<double> d64;
+  PlanData<float> d32;
+  // scratch: two 6-field work buffers per vector, sized for complex128
+  void* d_work = nullptr;
+  size_t work_vecs = 0;
+  // small device buffers
+  int* d_inst = nullptr;
+  size_t inst_cap = 0;
+  double* d_red = nullptr;            // reduction scratch
+  size_t red_cap = 0;
+  // host staging for FAME_HOST_PTR calls
+  void* d_stage = nullptr;
+  size_t stage_bytes = 0;
+  std::string last_error;
+  // named grow-only device workspaces of the solvers
+  std::vector<void*> ws_ptr;
+  std::vector<size_t> ws_size;
+};
+
+// Workspace slot `id` of at least `bytes` bytes (contents not preserved on growth).
+void* workspace(Plan& P, int id, size_t bytes, cudaError_t* err);
+void free_workspaces(Plan& P);
+cudaError_t ensure_work(Plan& P, size_t vecs);
+int fail(Plan* P, int code, const std::string& msg);
+int cuda_fail(Plan* P, cudaError_t e, const char* where);
+
+// ---- kernel launchers (fncb_kernels.cu) ----
+template <class R>
+cudaError_t launch_fncB(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,
+                        cx<R>* w0, cx<R>* w1, cudaStream_t st);
+template <class R>
+cudaError_t launch_fncA(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,
+                        cudaStream_t st);
+// MtxVecMul_FFT on 3Nq vectors: trans = 0 'notranspose' (S .* ifftn*sqrt(N)),
+// 1 'transpose' (fftn(conj(S).*x)/sqrt(N)).
+template <class R>
+cudaError_t launch_transform(const Plan& P, int trans, const cx<R>* x, cx<R>* y, int nvec,
+                             const VecCtx& ctx, cudaStream_t st);
+// Composed handles: which = 0 Pr, 1 Qr (2Nq -> 3Nq), 2 Prs, 3 Qrs (3Nq -> 2Nq)
+template <class R>
+cudaError_t launch_handle(const Plan& P, int which, const cx<R>* x, cx<R>* y, int nvec,
+                          const VecCtx& ctx, cx<R>* w0, cudaStream_t st);
+// Material operator alone on spatial 6-field vectors (periodic frame, no S):
+// [u'; v'] = [M J^H; J N] [u; v], the middle factor of fncB.
+template <class R>
+cudaError_t launch_material(const Plan& P, const cx<R>* uv, cx<R>* out, int nvec,
+                            const VecCtx& ctx, cx<R>* w1, cudaStream_t st);
+
+bool n_supported(int n);
+
+}  // namespace fame
+
+// The opaque handle of the C ABI.
+struct fame_plan_s {
+  fame::Plan P;
+};

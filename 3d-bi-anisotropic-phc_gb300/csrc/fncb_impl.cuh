@@ -1,0 +1,392 @@
+// Kernels of the curl-SVD transforms and of the fncB operator.
+//
+// fncB (reference: fun_Lanczos/fncB.m:3-6) on a quasi-periodic n^3 grid is
+//   y = blkdiag(Pr, Qr)^H * [M J^H; J N] * blkdiag(Pr, Qr) * x
+// with Pr = Psi*Pi.Pr, Qr = Phi*Pi.Qr (Funhand_Generate_Lanzcos.m:79-82) and
+// Psi = Phi = S .* unitary-inverse-DFT per component (gMtxVecMul_FFT.m:10-36).
+// The Bloch phase S is diagonal and the interpolated material operators are
+// built from Bloch shifts T_d, so S^H T_d S = tau_d P_d with P_d the periodic
+// shift and tau_d = exp(i theta_d / n).  fncB therefore runs entirely in the
+// periodic frame: S is never applied, and every shift carries the constant
+// phase tau_d.
+//
+// Material operators (IntCovarForm{N_vertex,M_vertex_new,J_vertex_new}.m and
+// the symmetrisation in Interpolation_Material_Matrix_Mult_Point_vertex.m:22-26)
+// factor into  edge/face -> vertex gathers, a per-vertex 3x3 tensor product,
+// and vertex -> edge/face scatters:
+//   U_j = 1/4 (I+T_a)^H (I+T_b)^H u_j   (a, b = axes != j)   face -> vertex
+//   V_j = 1/2 (I+T_j)^H v_j                                  edge -> vertex
+//   Hu_i = sum_{j!=i} Mh_ij U_j + sum_j conj(J_ji) V_j
+//   Hv_i = sum_{j!=i} Nh_ij V_j + sum_j J_ij U_j
+//   u'_i = m_i u_i + 1/4 (I+T_a)(I+T_b) Hu_i ,  m_i = face average of Re Mh_ii
+//   v'_i = n_i v_i + 1/2 (I+T_i) Hv_i        ,  n_i = edge average of Re Nh_ii
+// where Mh, Nh are the Hermitian parts of the vertex tensors: (X + X^H)/2 of
+// the assembled operator equals the operator built from Herm(A).
+//
+// Pipeline (this file, one launch each):
+//   plane_inv  : Pi blocks per frequency voxel + inverse DFT along x and y
+//   col        : inverse DFT along z (in place)
+//   vertex     : U, V, Hu, Hv at every vertex
+//   faceedge   : u', v' (in place over u, v)
+//   col        : forward DFT along z
+//   plane_fwd  : forward DFT along y and x + Pi^H blocks
+//
+// This header holds the size-templated kernels; fncb_inst_*.cu instantiate
+// them per precision and grid size so the size list compiles in parallel,
+// and fncb_stencil.cu holds the size-independent kernels and the dispatch.
+#pragma once
+
+#include "fame_internal.h"
+#include "fft_reg.cuh"
+
+namespace fame {
+namespace detail {
+
+
+constexpr double kInvSqrt14 = 0.26726124191242438468455348087975;
+
+template <class R> struct PiBlock {
+  cx<R> p1[3], p2[3];
+  R sig;
+};
+
+// SVD_Matrix_curl.m:45-57 for one frequency voxel: with L = (Lx, Ly, Lz),
+// w = (1,2,3)/sqrt(14):  Pi1 = (conj(L) x w)/|conj(L) x w|,
+// Pi2 = (conj(Pi1) x conj(L))/|L|, Sigma = |L|.
+template <class R>
+__device__ __forceinline__ PiBlock<R> pi_block(cx<R> lx, cx<R> ly, cx<R> lz) {
+  const R w1 = R(1 * kInvSqrt14), w2 = R(2 * kInvSqrt14), w3 = R(3 * kInvSqrt14);
+  R lq = lx.x * lx.x + lx.y * lx.y + ly.x * ly.x + ly.y * ly.y + lz.x * lz.x + lz.y * lz.y;
+  cx<R> lw = mk<R>(w1 * lx.x + w2 * ly.x + w3 * lz.x, w1 * lx.y + w2 * ly.y + w3 * lz.y);
+  R n1sq = lq - (lw.x * lw.x + lw.y * lw.y);
+  R inv1 = R(1) / sqrt(n1sq);
+  R sq = sqrt(lq);
+  R inv0 = R(1) / sq;
+  cx<R> b0 = cconj(lx), b1 = cconj(ly), b2 = cconj(lz);
+  PiBlock<R> P;
+  P.p1[0] = cscale(csub(cscale(b1, w3), cscale(b2, w2)), inv1);
+  P.p1[1] = cscale(csub(cscale(b2, w1), cscale(b0, w3)), inv1);
+  P.p1[2] = cscale(csub(cscale(b0, w2), cscale(b1, w1)), inv1);
+  cx<R> c0 = cconj(P.p1[0]), c1 = cconj(P.p1[1]), c2 = cconj(P.p1[2]);
+  P.p2[0] = cscale(csub(cmul(c1, b2), cmul(c2, b1)), inv0);
+  P.p2[1] = cscale(csub(cmul(c2, b0), cmul(c0, b2)), inv0);
+  P.p2[2] = cscale(csub(cmul(c0, b1), cmul(c1, b0)), inv0);
+  P.sig = sq;
+  return P;
+}
+
+template <class R> __device__ __forceinline__ R rsqrt_n3(int n) {
+  return R(1) / sqrt(R(n) * R(n) * R(n));
+}
+
+// ---------------------------------------------------------------------------
+// plane_inv: one CTA per (k3 plane, side, vector); 3N threads.
+// PREP: build the 3 frequency components of one side from (a, b):
+//   side 0 (Pr):  p = -conj(Pi2) a + conj(Pi1) b      (Pi.Pr, SVD_Matrix_curl.m:64)
+//   side 1 (Qr):  q =  Pi1 a + Pi2 b                  (Pi.Qr, SVD_Matrix_curl.m:63)
+// else copy 3 components.  Then inverse DFT along x (rows, via shared
+// memory) and y (columns, straight to global), scale by 1/n, and multiply by
+// S_x S_y when WITH_S.
+// ---------------------------------------------------------------------------
+template <class R, int N, bool PREP, bool WITH_S>
+__global__ void __launch_bounds__(3 * N < 32 ? 32 : 3 * N)
+k_plane_inv(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d, VecCtx ctx,
+            long long in_stride, long long in_side_stride, long long out_stride, int side0) {
+  constexpr int LD = N + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);  // [3][N][LD]
+  const int k3 = blockIdx.x;
+  const int vec = blockIdx.z;
+  if (ctx.active && !ctx.active[vec]) return;
+  const int inst = vec_inst(ctx, vec);
+  const int side = side0 + blockIdx.y;
+  const long long Nq = (long long)N * N * N;
+  const cx<R>* lam = d.lam + (long long)inst * 3 * N;
+  const cx<R>* xin = x + vec * in_stride + blockIdx.y * in_side_stride + (long long)k3 * N * N;
+  const int tid = threadIdx.x;
+
+  for (int e = tid; e < N * N; e += blockDim.x) {
+    const int i2 = e / N, i1 = e - i2 * N;
+    cx<R> v0, v1, v2;
+    if constexpr (PREP) {
+      PiBlock<R> P = pi_block<R>(lam[i1], lam[N + i2], lam[2 * N + k3]);
+      cx<R> a = xin[e], b = xin[Nq + e];
+      if (side == 0) {
+        v0 = cfmac(P.p1[0], b, cneg(cmulc(P.p2[0], a)));
+        v1 = cfmac(P.p1[1], b, cneg(cmulc(P.p2[1], a)));
+        v2 = cfmac(P.p1[2], b, cneg(cmulc(P.p2[2], a)));
+      } else {
+        v0 = cfma(P.p2[0], b, cmul(P.p1[0], a));
+        v1 = cfma(P.p2[1], b, cmul(P.p1[1], a));
+        v2 = cfma(P.p2[2], b, cmul(P.p1[2], a));
+      }
+    } else {
+      v0 = xin[e];
+      v1 = xin[Nq + e];
+      v2 = xin[2 * Nq + e];
+    }
+    sm[(0 * N + i2) * LD + i1] = v0;
+    sm[(1 * N + i2) * LD + i1] = v1;
+    sm[(2 * N + i2) * LD + i1] = v2;
+  }
+  __syncthreads();
+  if (tid < 3 * N) {  // x rows
+    const int c = tid / N, i2 = tid - c * N;
+    cx<R>* row = sm + (c * N + i2) * LD;
+    cx<R> v[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = row[i];
+    fft<R, N, +1>(v);
+#pragma unroll
+    for (int i = 0; i < N; ++i) row[i] = v[i];
+  }
+  __syncthreads();
+  if (tid < 3 * N) {  // y columns
+    const int c = tid / N, i1 = tid - c * N;
+    cx<R> v[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = sm[(c * N + i) * LD + i1];
+    fft<R, N, +1>(v);
+    const R scale = R(1) / R(N);
+    cx<R> sx = mk<R>(R(1), R(0));
+    const cx<R>* S = d.sxyz + (long long)inst * 3 * N;
+    if constexpr (WITH_S) sx = S[i1];
+    cx<R>* o = out + vec * out_stride + (long long)(blockIdx.y * 3 + c) * Nq + (long long)k3 * N * N + i1;
+#pragma unroll
+    for (int i2 = 0; i2 < N; ++i2) {
+      cx<R> r = cscale(v[i2], scale);
+      if constexpr (WITH_S) r = cmul(r, cmul(sx, S[N + i2]));
+      o[(long long)i2 * N] = r;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// plane_fwd: one CTA per (k3 plane, side, vector); 3N threads.
+// Forward DFT along y (columns, straight from global) and x (rows, shared
+// memory), scale 1/n; WITH_S multiplies conj(S_x S_y) first.  POST applies
+// the Pi^H blocks of one side (SVD_Matrix_curl.m:63-64, handles Prs/Qrs):
+//   side 0 (Prs): a = -sum_c Pi2_c u_c,  b = sum_c Pi1_c u_c
+//   side 1 (Qrs): a = sum_c conj(Pi1_c) v_c, b = sum_c conj(Pi2_c) v_c
+// else copies the 3 components out.
+// ---------------------------------------------------------------------------
+template <class R, int N, bool POST, bool WITH_S>
+__global__ void __launch_bounds__(3 * N < 32 ? 32 : 3 * N)
+k_plane_fwd(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, VecCtx ctx,
+            long long w_stride, long long out_stride, long long out_side_stride, int side0) {
+  constexpr int LD = N + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);  // [3][N][LD]
+  const int k3 = blockIdx.x;
+  const int vec = blockIdx.z;
+  if (ctx.active && !ctx.active[vec]) return;
+  const int inst = vec_inst(ctx, vec);
+  const int side = side0 + blockIdx.y;
+  const long long Nq = (long long)N * N * N;
+  const int tid = threadIdx.x;
+  const cx<R>* S = d.sxyz + (long long)inst * 3 * N;
+  if (tid < 3 * N) {  // y columns
+    const int c = tid / N, i1 = tid - c * N;
+    const cx<R>* src = w + vec * w_stride + (long long)(blockIdx.y * 3 + c) * Nq + (long long)k3 * N * N + i1;
+    cx<R> v[N];
+    cx<R> sx = mk<R>(R(1), R(0));
+    if constexpr (WITH_S) sx = S[i1];
+#pragma unroll
+    for (int i2 = 0; i2 < N; ++i2) {
+      v[i2] = src[(long long)i2 * N];
+      if constexpr (WITH_S) v[i2] = cmulc(cmul(sx, S[N + i2]), v[i2]);
+    }
+    fft<R, N, -1>(v);
+#pragma unroll
+    for (int i2 = 0; i2 < N; ++i2) sm[(c * N + i2) * LD + i1] = v[i2];
+  }
+  __syncthreads();
+  if (tid < 3 * N) {  // x rows
+    const int c = tid / N, i2 = tid - c * N;
+    cx<R>* row = sm + (c * N + i2) * LD;
+    cx<R> v[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = row[i];
+    fft<R, N, -1>(v);
+    const R scale = R(1) / R(N);
+#pragma unroll
+    for (int i = 0; i < N; ++i) row[i] = cscale(v[i], scale);
+  }
+  __syncthreads();
+  const cx<R>* lam = d.lam + (long long)inst * 3 * N;
+  cx<R>* o = y + vec * out_stride + blockIdx.y * out_side_stride + (long long)k3 * N * N;
+  for (int e = tid; e < N * N; e += blockDim.x) {
+    const int i2 = e / N, i1 = e - i2 * N;
+    cx<R> u0 = sm[(0 * N + i2) * LD + i1];
+    cx<R> u1 = sm[(1 * N + i2) * LD + i1];
+    cx<R> u2 = sm[(2 * N + i2) * LD + i1];
+    if constexpr (POST) {
+      PiBlock<R> P = pi_block<R>(lam[i1], lam[N + i2], lam[2 * N + k3]);
+      cx<R> a, b;
+      if (side == 0) {
+        a = cneg(cfma(P.p2[2], u2, cfma(P.p2[1], u1, cmul(P.p2[0], u0))));
+        b = cfma(P.p1[2], u2, cfma(P.p1[1], u1, cmul(P.p1[0], u0)));
+      } else {
+        a = cfmac(P.p1[2], u2, cfmac(P.p1[1], u1, cmulc(P.p1[0], u0)));
+        b = cfmac(P.p2[2], u2, cfmac(P.p2[1], u1, cmulc(P.p2[0], u0)));
+      }
+      o[e] = a;
+      o[Nq + e] = b;
+    } else {
+      o[e] = u0;
+      o[Nq + e] = u1;
+      o[2 * Nq + e] = u2;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// col: DFT along z of every (i1, i2) column, in place; one thread per column.
+// SMODE 1: multiply S_z(i3) after (inverse); 2: multiply conj(S_z(i3)) before
+// (forward).  Scale 1/sqrt(n).
+// ---------------------------------------------------------------------------
+template <class R, int N, int DIR, int SMODE>
+__global__ void __launch_bounds__(128)
+k_col(cx<R>* __restrict__ w, PlanData<R> d, VecCtx ctx, long long stride) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = blockIdx.y;
+  const int vec = blockIdx.z;
+  if (col >= N * N) return;
+  if (ctx.active && !ctx.active[vec]) return;
+  const long long Nq = (long long)N * N * N;
+  cx<R>* p = w + vec * stride + (long long)f * Nq + col;
+  const cx<R>* Sz = d.sxyz + (long long)vec_inst(ctx, vec) * 3 * N + 2 * N;
+  cx<R> v[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    v[i] = p[(long long)i * N * N];
+    if constexpr (SMODE == 2) v[i] = cmulc(Sz[i], v[i]);
+  }
+  fft<R, N, DIR>(v);
+  const R scale = R(1) / sqrt(R(N));
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    cx<R> r = cscale(v[i], scale);
+    if constexpr (SMODE == 1) r = cmul(Sz[i], r);
+    p[(long long)i * N * N] = r;
+  }
+}
+
+inline dim3 grid_pts(long long Nq, int nvec, int tpb) {
+  return dim3((unsigned)((Nq + tpb - 1) / tpb), (unsigned)nvec, 1);
+}
+
+template <class R, int N, bool PREP, bool WITH_S>
+cudaError_t plane_inv(const Plan& P, const PlanData<R>& d, const cx<R>* x, cx<R>* out, int nvec,
+                      int nside, int side0, long long in_stride, long long in_side_stride,
+                      long long out_stride, const VecCtx& ctx, cudaStream_t st) {
+  const int threads = ((3 * N + 31) / 32) * 32;
+  const size_t sm = sizeof(cx<R>) * 3 * N * (N + 1);
+  auto kfn = k_plane_inv<R, N, PREP, WITH_S>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  kfn<<<dim3(N, nside, nvec), threads, sm, st>>>(x, out, d, ctx, in_stride, in_side_stride, out_stride,
+                                                 side0);
+  return cudaGetLastError();
+}
+
+template <class R, int N, bool POST, bool WITH_S>
+cudaError_t plane_fwd(const Plan& P, const PlanData<R>& d, const cx<R>* w, cx<R>* y, int nvec, int nside,
+                      int side0, long long w_stride, long long out_stride, long long out_side_stride,
+                      const VecCtx& ctx, cudaStream_t st) {
+  const int threads = ((3 * N + 31) / 32) * 32;
+  const size_t sm = sizeof(cx<R>) * 3 * N * (N + 1);
+  auto kfn = k_plane_fwd<R, N, POST, WITH_S>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  kfn<<<dim3(N, nside, nvec), threads, sm, st>>>(w, y, d, ctx, w_stride, out_stride, out_side_stride,
+                                                 side0);
+  return cudaGetLastError();
+}
+
+template <class R, int N, int DIR, int SMODE>
+cudaError_t col(const PlanData<R>& d, cx<R>* w, int nfield, int nvec, long long stride, const VecCtx& ctx,
+                cudaStream_t st) {
+  dim3 g((N * N + 127) / 128, nfield, nvec);
+  k_col<R, N, DIR, SMODE><<<g, 128, 0, st>>>(w, d, ctx, stride);
+  return cudaGetLastError();
+}
+
+template <class R> inline const PlanData<R>& pdata(const Plan& P);
+template <> inline const PlanData<double>& pdata<double>(const Plan& P) { return P.d64; }
+template <> inline const PlanData<float>& pdata<float>(const Plan& P) { return P.d32; }
+
+// Material stencil (fncb_stencil.cu): periodic-frame [M J^H; J N] in place on w0, scratch w1.
+template <class R>
+cudaError_t stencil(const Plan& P, cx<R>* w0, cx<R>* w1, int nvec, const VecCtx& ctx, cudaStream_t st);
+
+template <class R, int N>
+cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx, cx<R>* w0, cx<R>* w1,
+                   cudaStream_t st) {
+  const PlanData<R>& d = pdata<R>(P);
+  const long long Nq = P.Nq;
+  cudaError_t e;
+  e = plane_inv<R, N, true, false>(P, d, x, w0, nvec, 2, 0, 4 * Nq, 2 * Nq, 6 * Nq, ctx, st);
+  if (e != cudaSuccess) return e;
+  e = col<R, N, +1, 0>(d, w0, 6, nvec, 6 * Nq, ctx, st);
+  if (e != cudaSuccess) return e;
+  e = stencil<R>(P, w0, w1, nvec, ctx, st);
+  if (e != cudaSuccess) return e;
+  e = col<R, N, -1, 0>(d, w0, 6, nvec, 6 * Nq, ctx, st);
+  if (e != cudaSuccess) return e;
+  return plane_fwd<R, N, true, false>(P, d, w0, y, nvec, 2, 0, 6 * Nq, 4 * Nq, 2 * Nq, ctx, st);
+}
+
+template <class R, int N>
+cudaError_t transform_n(const Plan& P, int trans, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,
+                        cudaStream_t st) {
+  const PlanData<R>& d = pdata<R>(P);
+  const long long Nq = P.Nq;
+  cudaError_t e;
+  if (trans == 0) {
+    e = plane_inv<R, N, false, true>(P, d, x, y, nvec, 1, 0, 3 * Nq, 0, 3 * Nq, ctx, st);
+    if (e != cudaSuccess) return e;
+    return col<R, N, +1, 1>(d, y, 3, nvec, 3 * Nq, ctx, st);
+  }
+  // transpose: z first (conj(S_z) before), then y, x with conj(S_x S_y) before.
+  if (x != y) {
+    e = cudaMemcpyAsync(y, x, sizeof(cx<R>) * 3 * Nq * nvec, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return e;
+  }
+  e = col<R, N, -1, 2>(d, y, 3, nvec, 3 * Nq, ctx, st);
+  if (e != cudaSuccess) return e;
+  return plane_fwd<R, N, false, true>(P, d, y, y, nvec, 1, 0, 3 * Nq, 3 * Nq, 0, ctx, st);
+}
+
+template <class R, int N>
+cudaError_t handle_n(const Plan& P, int which, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,
+                     cx<R>* w0, cudaStream_t st) {
+  const PlanData<R>& d = pdata<R>(P);
+  const long long Nq = P.Nq;
+  cudaError_t e;
+  if (which == 0 || which == 1) {  // Pr / Qr : 2Nq -> 3Nq
+    e = plane_inv<R, N, true, true>(P, d, x, y, nvec, 1, which, 2 * Nq, 0, 3 * Nq, ctx, st);
+    if (e != cudaSuccess) return e;
+    return col<R, N, +1, 1>(d, y, 3, nvec, 3 * Nq, ctx, st);
+  }
+  // Prs / Qrs : 3Nq -> 2Nq through the 3Nq scratch w0
+  e = cudaMemcpyAsync(w0, x, sizeof(cx<R>) * 3 * Nq * nvec, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  e = col<R, N, -1, 2>(d, w0, 3, nvec, 3 * Nq, ctx, st);
+  if (e != cudaSuccess) return e;
+  return plane_fwd<R, N, true, true>(P, d, w0, y, nvec, 1, which - 2, 3 * Nq, 2 * Nq, 0, ctx, st);
+}
+
+
+}  // namespace detail
+}  // namespace fame
+
+#define FAME_SIZE_SIGS(R, NN)                                                                                      \
+  cudaError_t fame::detail::fncB_n<R, NN>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&, cx<R>*, cx<R>*,   \
+                                          cudaStream_t);                                                           \
+  template cudaError_t fame::detail::transform_n<R, NN>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&, \
+                                                        cudaStream_t);                                             \
+  template cudaError_t fame::detail::handle_n<R, NN>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&,    \
+                                                     cx<R>*, cudaStream_t);
+// explicit instantiation of one (precision, size)
+#define FAME_INST_SIZE(R, NN) template FAME_SIZE_SIGS(R, NN)

@@ -1,0 +1,54 @@
+// Krylov glue launchers (krylov_kernels.cu) and host drivers (solvers.cu).
+#pragma once
+
+#include "fame_internal.h"
+
+namespace fame {
+
+// out[v*ma + m] = sum_i conj(a[v][m][i]) * b[v][i]  (FP64 accumulation)
+template <class R>
+cudaError_t dot_batched(const cx<R>* a, long long a_vstride, long long a_cstride, int ma, const cx<R>* b,
+                        long long b_vstride, long long len, int nvec, double2* out, double2* partial, int nblk,
+                        const int* active, cudaStream_t st);
+template <class R>
+cudaError_t axpby_batched(const cx<R>* x, cx<R>* y, long long len, long long stride, int nvec,
+                          const double2* alpha, const double2* beta, const int* active, cudaStream_t st);
+template <class R>
+cudaError_t cg_xr(cx<R>* x, cx<R>* r, const cx<R>* p, const cx<R>* q, long long len, long long stride, int nvec,
+                  const double* alpha, const int* active, cudaStream_t st);
+template <class R>
+cudaError_t cg_p(cx<R>* p, const cx<R>* r, long long len, long long stride, int nvec, const double* beta,
+                 const int* active, cudaStream_t st);
+cudaError_t cg_scalars(int stage, int nvec, const double2* dot, double* rho, double* alpha, double* beta,
+                       const double* tol2b2, int* active, int* iters, double* res2, int it, cudaStream_t st);
+template <class R>
+cudaError_t block_rot(const cx<R>* in, cx<R>* out, long long len, long long ld, int p, int k, const double* U,
+                      cudaStream_t st);
+template <class R>
+cudaError_t sub_combo(cx<R>* r, const cx<R>* X, long long len, long long ld, int m, const double2* c,
+                      cudaStream_t st);
+template <class D, class S>
+cudaError_t convert(const cx<S>* in, cx<D>* out, long long n, cudaStream_t st);
+cudaError_t refine_acc(double2* x, const float2* d, long long len, int nvec, const int* active, cudaStream_t st);
+cudaError_t residual(const double2* b, const double2* bx, double2* res, float2* res32, long long len, int nvec,
+                     const int* active, cudaStream_t st);
+template <class R>
+cudaError_t scale_batched(const cx<R>* x, cx<R>* y, long long len, int nvec, const double* s, const int* active,
+                          cudaStream_t st);
+
+// Host drivers (solvers.cu).
+// Batched CG on B (fncinvB).  h_mask (host, may be null) selects the vectors
+// to solve; others are left untouched.  iters_out / relres_out (host, may be
+// null) receive per-vector results; a negative iteration count marks a
+// breakdown or a non-finite residual.
+template <class R>
+int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, double tol, int maxit,
+                int* iters_out, double* relres_out, const unsigned char* h_mask = nullptr);
+
+// Mixed-precision B^{-1}: complex64 CG corrections inside FP64 residual
+// refinement until ||b - B x|| <= tol ||b|| (FP64).  Bx receives B*x (FP64).
+int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, const int* d_inst, double tol,
+                  int max_rounds, double inner_tol32, int maxit32, const unsigned char* h_mask,
+                  long long* cg_iters, long long* b64_applies);
+
+}  // namespace fame

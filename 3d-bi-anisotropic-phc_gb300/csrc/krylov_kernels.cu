@@ -1,0 +1,360 @@
+// Vector kernels of the Krylov glue: batched complex dot products with FP64
+// accumulation, the fused conjugate-gradient updates of fncinvB (pcg), and
+// the block Gram-Schmidt / restart products of the Lanczos band solver.
+// Every kernel works on a batch of vectors, one vector per k-point instance,
+// and skips vectors whose `active` flag is 0.
+#include "krylov.h"
+
+namespace fame {
+namespace {
+
+constexpr int kRedThreads = 256;
+
+// Block-wide sum of a (double re, double im) pair; result valid in thread 0.
+__device__ __forceinline__ double2 block_sum2(double2 v) {
+  __shared__ double2 sh[kRedThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < (blockDim.x >> 5) ? sh[lane] : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+  }
+  return v;
+}
+
+// partial[v][m][blk] = sum over the block's slice of conj(a_m) * b
+// a: nvec x ma vectors (stride lda per column, cols per vector = ma), b: one vector per vec.
+template <class R>
+__global__ void __launch_bounds__(kRedThreads)
+k_dot_partial(const cx<R>* __restrict__ a, long long a_vstride, long long a_cstride, int ma,
+              const cx<R>* __restrict__ b, long long b_vstride, long long len, double2* __restrict__ partial,
+              const int* __restrict__ active) {
+  const int vec = blockIdx.y;
+  const int m = blockIdx.z;
+  const int nblk = gridDim.x;
+  double2* out = partial + ((long long)vec * ma + m) * nblk + blockIdx.x;
+  if (active && !active[vec]) {
+    if (threadIdx.x == 0) *out = make_double2(0.0, 0.0);
+    return;
+  }
+  const cx<R>* av = a + vec * a_vstride + m * a_cstride;
+  const cx<R>* bv = b + vec * b_vstride;
+  double2 s = make_double2(0.0, 0.0);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)nblk * blockDim.x) {
+    cx<R> x = av[i], y = bv[i];
+    s.x += double(x.x) * double(y.x) + double(x.y) * double(y.y);
+    s.y += double(x.x) * double(y.y) - double(x.y) * double(y.x);
+  }
+  s = block_sum2(s);
+  if (threadIdx.x == 0) *out = s;
+}
+
+__global__ void __launch_bounds__(kRedThreads)
+k_dot_final(const double2* __restrict__ partial, int nblk, double2* __restrict__ out) {
+  const long long row = blockIdx.x;  // vec * ma + m
+  double2 s = make_double2(0.0, 0.0);
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
+    double2 p = partial[row * nblk + i];
+    s.x += p.x;
+    s.y += p.y;
+  }
+  s = block_sum2(s);
+  if (threadIdx.x == 0) out[row] = s;
+}
+
+// y_v = alpha_v * x_v + beta_v * y_v with per-vector complex scalars (FP64)
+template <class R>
+__global__ void k_axpby(const cx<R>* __restrict__ x, cx<R>* __restrict__ y, long long len, long long stride,
+                        const double2* __restrict__ alpha, const double2* __restrict__ beta,
+                        const int* __restrict__ active) {
+  const int vec = blockIdx.y;
+  if (active && !active[vec]) return;
+  const double2 a = alpha[vec], bb = beta[vec];
+  const cx<R>* xv = x + vec * stride;
+  cx<R>* yv = y + vec * stride;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    cx<R> xi = xv[i], yi = yv[i];
+    double rx = a.x * xi.x - a.y * xi.y + bb.x * yi.x - bb.y * yi.y;
+    double ry = a.x * xi.y + a.y * xi.x + bb.x * yi.y + bb.y * yi.x;
+    yv[i] = mk<R>(R(rx), R(ry));
+  }
+}
+
+// CG update: x += a p ; r -= a q  with a = rho / Re(p'q) per vector.
+template <class R>
+__global__ void k_cg_xr(cx<R>* __restrict__ x, cx<R>* __restrict__ r, const cx<R>* __restrict__ p,
+                        const cx<R>* __restrict__ q, long long len, long long stride,
+                        const double* __restrict__ alpha, const int* __restrict__ active) {
+  const int vec = blockIdx.y;
+  if (active && !active[vec]) return;
+  const R a = R(alpha[vec]);
+  const long long o = vec * stride;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    cx<R> pi = p[o + i], qi = q[o + i], xi = x[o + i], ri = r[o + i];
+    xi.x += a * pi.x; xi.y += a * pi.y;
+    ri.x -= a * qi.x; ri.y -= a * qi.y;
+    x[o + i] = xi;
+    r[o + i] = ri;
+  }
+}
+
+// p = r + beta p
+template <class R>
+__global__ void k_cg_p(cx<R>* __restrict__ p, const cx<R>* __restrict__ r, long long len, long long stride,
+                       const double* __restrict__ beta, const int* __restrict__ active) {
+  const int vec = blockIdx.y;
+  if (active && !active[vec]) return;
+  const R b = R(beta[vec]);
+  const long long o = vec * stride;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    cx<R> pi = p[o + i], ri = r[o + i];
+    p[o + i] = mk<R>(ri.x + b * pi.x, ri.y + b * pi.y);
+  }
+}
+
+// Per-vector CG scalars.  stage 0: alpha = rho/Re(pq); stage 1: convergence
+// test on rho_new and beta = rho_new/rho.
+__global__ void k_cg_scalars(int stage, int nvec, const double2* __restrict__ dot, double* __restrict__ rho,
+                             double* __restrict__ alpha, double* __restrict__ beta,
+                             const double* __restrict__ tol2b2, int* __restrict__ active,
+                             int* __restrict__ iters, double* __restrict__ res2, int it) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nvec || !active[v]) return;
+  if (stage == 0) {
+    const double pq = dot[v].x;
+    alpha[v] = (pq != 0.0 && isfinite(pq)) ? rho[v] / pq : 0.0;
+    if (!(pq > 0.0) || !isfinite(pq)) {  // breakdown: B must be HPD
+      active[v] = 0;
+      iters[v] = -it;
+    }
+  } else {
+    const double rn = dot[v].x;
+    res2[v] = rn;
+    beta[v] = rho[v] != 0.0 ? rn / rho[v] : 0.0;
+    rho[v] = rn;
+    iters[v] = it;
+    if (!isfinite(rn)) {  // NaN / Inf: stop and flag
+      active[v] = 0;
+      iters[v] = -it;
+    } else if (rn <= tol2b2[v]) {
+      active[v] = 0;  // converged: ||r|| <= tol ||b||
+    }
+  }
+}
+
+// out[:, j] = sum_i in[:, i] * U[i, j]  (U real, p x k, column-major), all columns of one vector block
+template <class R>
+__global__ void k_block_rot(const cx<R>* __restrict__ in, cx<R>* __restrict__ out, long long len,
+                            long long ld, int p, int k, const double* __restrict__ U) {
+  extern __shared__ double Us[];
+  for (int i = threadIdx.x; i < p * k; i += blockDim.x) Us[i] = U[i];
+  __syncthreads();
+  for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < len; row += (long long)gridDim.x * blockDim.x) {
+    for (int j = 0; j < k; ++j) {
+      double sx = 0.0, sy = 0.0;
+      for (int i = 0; i < p; ++i) {
+        cx<R> q = in[(long long)i * ld + row];
+        sx += double(q.x) * Us[j * p + i];
+        sy += double(q.y) * Us[j * p + i];
+      }
+      out[(long long)j * ld + row] = mk<R>(R(sx), R(sy));
+    }
+  }
+}
+
+// r -= sum_i c_i X[:, i]  (complex coefficients, FP64)
+template <class R>
+__global__ void k_sub_combo(cx<R>* __restrict__ r, const cx<R>* __restrict__ X, long long len, long long ld, int m,
+                            const double2* __restrict__ c) {
+  extern __shared__ double2 cs[];
+  for (int i = threadIdx.x; i < m; i += blockDim.x) cs[i] = c[i];
+  __syncthreads();
+  for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < len; row += (long long)gridDim.x * blockDim.x) {
+    cx<R> acc = r[row];
+    double ax = acc.x, ay = acc.y;
+    for (int i = 0; i < m; ++i) {
+      cx<R> q = X[(long long)i * ld + row];
+      ax -= cs[i].x * q.x - cs[i].y * q.y;
+      ay -= cs[i].x * q.y + cs[i].y * q.x;
+    }
+    r[row] = mk<R>(R(ax), R(ay));
+  }
+}
+
+template <class D, class S>
+__global__ void k_convert(const cx<S>* __restrict__ in, cx<D>* __restrict__ out, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = mk<D>(D(in[i].x), D(in[i].y));
+}
+
+// x64 += d32 ; res = b - bx (both FP64) for active vectors
+__global__ void k_refine_acc(double2* __restrict__ x, const float2* __restrict__ d, long long len,
+                             const int* __restrict__ active) {
+  const int vec = blockIdx.y;
+  if (active && !active[vec]) return;
+  const long long o = vec * len;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    double2 a = x[o + i];
+    float2 b = d[o + i];
+    a.x += b.x;
+    a.y += b.y;
+    x[o + i] = a;
+  }
+}
+__global__ void k_residual(const double2* __restrict__ b, const double2* __restrict__ bx, double2* __restrict__ res,
+                           float2* __restrict__ res32, long long len, const int* __restrict__ active) {
+  const int vec = blockIdx.y;
+  if (active && !active[vec]) return;
+  const long long o = vec * len;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    double2 r = make_double2(b[o + i].x - bx[o + i].x, b[o + i].y - bx[o + i].y);
+    res[o + i] = r;
+    res32[o + i] = make_float2(float(r.x), float(r.y));
+  }
+}
+// y = s_v * x per vector (real per-vector scalars), x and y may alias
+template <class R>
+__global__ void k_scale(const cx<R>* x, cx<R>* y, long long len, const double* __restrict__ s,
+                        const int* __restrict__ active) {
+  const int vec = blockIdx.y;
+  if (active && !active[vec]) return;
+  const R a = R(s[vec]);
+  const long long o = vec * len;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    cx<R> v = x[o + i];
+    y[o + i] = mk<R>(a * v.x, a * v.y);
+  }
+}
+
+int grid_for(long long len) {
+  long long b = (len + 255) / 256;
+  if (b > 4096) b = 4096;
+  return int(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+template <class R>
+cudaError_t dot_batched(const cx<R>* a, long long a_vstride, long long a_cstride, int ma, const cx<R>* b,
+                        long long b_vstride, long long len, int nvec, double2* out, double2* partial,
+                        int nblk, const int* active, cudaStream_t st) {
+  if (nvec <= 0 || ma <= 0) return cudaSuccess;
+  dim3 g(nblk, nvec, ma);
+  k_dot_partial<R><<<g, kRedThreads, 0, st>>>(a, a_vstride, a_cstride, ma, b, b_vstride, len, partial, active);
+  k_dot_final<<<nvec * ma, kRedThreads, 0, st>>>(partial, nblk, out);
+  return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t axpby_batched(const cx<R>* x, cx<R>* y, long long len, long long stride, int nvec,
+                          const double2* alpha, const double2* beta, const int* active, cudaStream_t st) {
+  if (nvec <= 0) return cudaSuccess;
+  int gx = grid_for(len);
+  if (gx > 1024) gx = 1024;
+  k_axpby<R><<<dim3(gx, nvec), 256, 0, st>>>(x, y, len, stride, alpha, beta, active);
+  return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t cg_xr(cx<R>* x, cx<R>* r, const cx<R>* p, const cx<R>* q, long long len, long long stride, int nvec,
+                  const double* alpha, const int* active, cudaStream_t st) {
+  int gx = grid_for(len);
+  if (gx > 1024) gx = 1024;
+  k_cg_xr<R><<<dim3(gx, nvec), 256, 0, st>>>(x, r, p, q, len, stride, alpha, active);
+  return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t cg_p(cx<R>* p, const cx<R>* r, long long len, long long stride, int nvec, const double* beta,
+                 const int* active, cudaStream_t st) {
+  int gx = grid_for(len);
+  if (gx > 1024) gx = 1024;
+  k_cg_p<R><<<dim3(gx, nvec), 256, 0, st>>>(p, r, len, stride, beta, active);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_scalars(int stage, int nvec, const double2* dot, double* rho, double* alpha, double* beta,
+                       const double* tol2b2, int* active, int* iters, double* res2, int it, cudaStream_t st) {
+  k_cg_scalars<<<(nvec + 127) / 128, 128, 0, st>>>(stage, nvec, dot, rho, alpha, beta, tol2b2, active, iters,
+                                                    res2, it);
+  return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t block_rot(const cx<R>* in, cx<R>* out, long long len, long long ld, int p, int k, const double* U,
+                      cudaStream_t st) {
+  k_block_rot<R><<<grid_for(len), 256, sizeof(double) * p * k, st>>>(in, out, len, ld, p, k, U);
+  return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t sub_combo(cx<R>* r, const cx<R>* X, long long len, long long ld, int m, const double2* c,
+                      cudaStream_t st) {
+  if (m <= 0) return cudaSuccess;
+  k_sub_combo<R><<<grid_for(len), 256, sizeof(double2) * m, st>>>(r, X, len, ld, m, c);
+  return cudaGetLastError();
+}
+
+template <class D, class S>
+cudaError_t convert(const cx<S>* in, cx<D>* out, long long n, cudaStream_t st) {
+  k_convert<D, S><<<grid_for(n), 256, 0, st>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t refine_acc(double2* x, const float2* d, long long len, int nvec, const int* active, cudaStream_t st) {
+  int gx = grid_for(len);
+  if (gx > 1024) gx = 1024;
+  k_refine_acc<<<dim3(gx, nvec), 256, 0, st>>>(x, d, len, active);
+  return cudaGetLastError();
+}
+
+cudaError_t residual(const double2* b, const double2* bx, double2* res, float2* res32, long long len, int nvec,
+                     const int* active, cudaStream_t st) {
+  int gx = grid_for(len);
+  if (gx > 1024) gx = 1024;
+  k_residual<<<dim3(gx, nvec), 256, 0, st>>>(b, bx, res, res32, len, active);
+  return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t scale_batched(const cx<R>* x, cx<R>* y, long long len, int nvec, const double* s, const int* active,
+                          cudaStream_t st) {
+  int gx = grid_for(len);
+  if (gx > 1024) gx = 1024;
+  k_scale<R><<<dim3(gx, nvec), 256, 0, st>>>(x, y, len, s, active);
+  return cudaGetLastError();
+}
+template cudaError_t scale_batched<double>(const cx<double>*, cx<double>*, long long, int, const double*, const int*,
+                                           cudaStream_t);
+template cudaError_t scale_batched<float>(const cx<float>*, cx<float>*, long long, int, const double*, const int*,
+                                          cudaStream_t);
+
+#define FAME_KINST(R)                                                                                     \
+  template cudaError_t dot_batched<R>(const cx<R>*, long long, long long, int, const cx<R>*, long long,  \
+                                      long long, int, double2*, double2*, int, const int*, cudaStream_t); \
+  template cudaError_t axpby_batched<R>(const cx<R>*, cx<R>*, long long, long long, int, const double2*, \
+                                        const double2*, const int*, cudaStream_t);                       \
+  template cudaError_t cg_xr<R>(cx<R>*, cx<R>*, const cx<R>*, const cx<R>*, long long, long long, int,   \
+                                const double*, const int*, cudaStream_t);                                 \
+  template cudaError_t cg_p<R>(cx<R>*, const cx<R>*, long long, long long, int, const double*,           \
+                               const int*, cudaStream_t);                                                 \
+  template cudaError_t block_rot<R>(const cx<R>*, cx<R>*, long long, long long, int, int, const double*, \
+                                    cudaStream_t);                                                        \
+  template cudaError_t sub_combo<R>(cx<R>*, const cx<R>*, long long, long long, int, const double2*,     \
+                                    cudaStream_t);
+FAME_KINST(float)
+FAME_KINST(double)
+template cudaError_t convert<float, double>(const cx<double>*, cx<float>*, long long, cudaStream_t);
+template cudaError_t convert<double, float>(const cx<float>*, cx<double>*, long long, cudaStream_t);
+
+}  // namespace fame

@@ -1,0 +1,612 @@
+// Host drivers of the Krylov glue: batched conjugate gradients on B
+// (fncinvB), the mixed-precision B^{-1} used by the complex64 band solve,
+// and the thick-restart Lanczos band solver of fun_Lanczos/Lanczos.m.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "krylov.h"
+#include "linalg_host.h"
+
+namespace fame {
+
+enum WsId {
+  WS_PCG_R = 0, WS_PCG_P, WS_PCG_Q, WS_PCG_SCAL, WS_PCG_PART,
+  WS_MIX_B32, WS_MIX_X32, WS_MIX_RES, WS_MIX_MASK,
+  WS_LZ_Q, WS_LZ_BQ, WS_LZ_VEC, WS_LZ_TMP, WS_LZ_COEF, WS_LZ_INST, WS_LZ_MASK, WS_LZ_U, WS_LZ_SCAL, WS_LZ_DOT,
+  WS_LZ_PART
+};
+
+#define FAME_CK(expr, where)                      \
+  do {                                            \
+    cudaError_t e_ = (expr);                      \
+    if (e_ != cudaSuccess) return cuda_fail(&P, e_, where); \
+  } while (0)
+
+static int dot_blocks(long long len, int nvec) {
+  long long target = (4LL * 152 + nvec - 1) / std::max(1, nvec);
+  long long maxb = (len + 2047) / 2048;
+  long long b = std::min(target, maxb);
+  if (b < 1) b = 1;
+  if (b > 512) b = 512;
+  return int(b);
+}
+
+// Device scalars of the batched CG, carved from one workspace.
+struct CgScalars {
+  double *rho, *alpha, *beta, *tol2b2, *res2;
+  int *active, *iters;
+  double2* dot;
+};
+
+template <class R>
+int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, double tol, int maxit, int* iters_out,
+                double* relres_out, const unsigned char* h_mask) {
+  if (nvec <= 0) return FAME_OK;
+  cudaStream_t st = P.stream;
+  const long long L = 4 * P.Nq;
+  const size_t vb = sizeof(cx<R>) * L * nvec;
+  cudaError_t e;
+  cx<R>* r = (cx<R>*)workspace(P, WS_PCG_R + (sizeof(R) == 4 ? 100 : 0), vb, &e);
+  FAME_CK(e, "pcg workspace");
+  cx<R>* p = (cx<R>*)workspace(P, WS_PCG_P + (sizeof(R) == 4 ? 100 : 0), vb, &e);
+  FAME_CK(e, "pcg workspace");
+  cx<R>* q = (cx<R>*)workspace(P, WS_PCG_Q + (sizeof(R) == 4 ? 100 : 0), vb, &e);
+  FAME_CK(e, "pcg workspace");
+  const size_t sb = (5 * sizeof(double) + 2 * sizeof(int) + sizeof(double2)) * nvec + 64;
+  char* s = (char*)workspace(P, WS_PCG_SCAL, sb, &e);
+  FAME_CK(e, "pcg workspace");
+  CgScalars S;
+  S.dot = (double2*)s;
+  S.rho = (double*)(S.dot + nvec);
+  S.alpha = S.rho + nvec;
+  S.beta = S.alpha + nvec;
+  S.tol2b2 = S.beta + nvec;
+  S.res2 = S.tol2b2 + nvec;
+  S.active = (int*)(S.res2 + nvec);
+  S.iters = S.active + nvec;
+  const int nblk = dot_blocks(L, nvec);
+  double2* part = (double2*)workspace(P, WS_PCG_PART, sizeof(double2) * nblk * nvec + 64, &e);
+  FAME_CK(e, "pcg workspace");
+  FAME_CK(ensure_work(P, nvec), "pcg fncB scratch");
+  cx<R>* w0 = (cx<R>*)P.d_work;
+  cx<R>* w1 = w0 + (size_t)nvec * 6 * P.Nq;
+
+  std::vector<int> act(nvec, 1);
+  if (h_mask)
+    for (int v = 0; v < nvec; ++v) act[v] = h_mask[v] ? 1 : 0;
+  FAME_CK(cudaMemcpyAsync(S.active, act.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
+  // ||b||^2 per vector
+  FAME_CK(dot_batched<R>(b, L, 0, 1, b, L, L, nvec, S.dot, part, nblk, S.active, st), "pcg dot");
+  std::vector<double2> bb(nvec);
+  FAME_CK(cudaMemcpyAsync(bb.data(), S.dot, sizeof(double2) * nvec, cudaMemcpyDeviceToHost, st), "pcg init");
+  FAME_CK(cudaStreamSynchronize(st), "pcg init");
+  std::vector<double> rho(nvec), t2(nvec);
+  for (int v = 0; v < nvec; ++v) {
+    rho[v] = bb[v].x;
+    t2[v] = tol * tol * bb[v].x;
+    if (act[v] && !(bb[v].x > 0.0)) {  // zero right-hand side: x = 0
+      act[v] = 0;
+    }
+  }
+  std::vector<int> it0(nvec, 0);
+  FAME_CK(cudaMemcpyAsync(S.rho, rho.data(), sizeof(double) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
+  FAME_CK(cudaMemcpyAsync(S.tol2b2, t2.data(), sizeof(double) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
+  FAME_CK(cudaMemcpyAsync(S.res2, rho.data(), sizeof(double) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
+  FAME_CK(cudaMemcpyAsync(S.iters, it0.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
+  for (int v = 0; v < nvec; ++v) {
+    const bool sel = h_mask ? h_mask[v] != 0 : true;
+    if (!sel) continue;
+    FAME_CK(cudaMemsetAsync(x + (size_t)v * L, 0, sizeof(cx<R>) * L, st), "pcg init");
+  }
+  FAME_CK(cudaMemcpyAsync(S.active, act.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
+  FAME_CK(cudaMemcpyAsync(r, b, vb, cudaMemcpyDeviceToDevice, st), "pcg init");
+  FAME_CK(cudaMemcpyAsync(p, b, vb, cudaMemcpyDeviceToDevice, st), "pcg init");
+  VecCtx ctx;
+  ctx.inst = d_inst;
+  ctx.active = S.active;
+  ctx.nk = P.nk;
+  const int chk = 4;
+  bool any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
+  for (int it = 1; it <= maxit && any; ++it) {
+    FAME_CK(launch_fncB<R>(P, p, q, nvec, ctx, w0, w1, st), "pcg fncB");
+    FAME_CK(dot_batched<R>(p, L, 0, 1, q, L, L, nvec, S.dot, part, nblk, S.active, st), "pcg dot");
+    FAME_CK(cg_scalars(0, nvec, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active, S.iters, S.res2, it, st), "pcg");
+    FAME_CK(cg_xr<R>(x, r, p, q, L, L, nvec, S.alpha, S.active, st), "pcg update");
+    FAME_CK(dot_batched<R>(r, L, 0, 1, r, L, L, nvec, S.dot, part, nblk, S.active, st), "pcg dot");
+    FAME_CK(cg_scalars(1, nvec, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active, S.iters, S.res2, it, st), "pcg");
+    FAME_CK(cg_p<R>(p, r, L, L, nvec, S.beta, S.active, st), "pcg update");
+    if (it % chk == 0 || it == maxit) {
+      FAME_CK(cudaMemcpyAsync(act.data(), S.active, sizeof(int) * nvec, cudaMemcpyDeviceToHost, st), "pcg check");
+      FAME_CK(cudaStreamSynchronize(st), "pcg check");
+      any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
+    }
+  }
+  std::vector<int> its(nvec);
+  std::vector<double> r2(nvec);
+  FAME_CK(cudaMemcpyAsync(its.data(), S.iters, sizeof(int) * nvec, cudaMemcpyDeviceToHost, st), "pcg out");
+  FAME_CK(cudaMemcpyAsync(r2.data(), S.res2, sizeof(double) * nvec, cudaMemcpyDeviceToHost, st), "pcg out");
+  FAME_CK(cudaMemcpyAsync(act.data(), S.active, sizeof(int) * nvec, cudaMemcpyDeviceToHost, st), "pcg out");
+  FAME_CK(cudaStreamSynchronize(st), "pcg out");
+  int rc = FAME_OK;
+  for (int v = 0; v < nvec; ++v) {
+    const bool sel = h_mask ? h_mask[v] != 0 : true;
+    if (!sel) continue;
+    if (iters_out) iters_out[v] = its[v];
+    if (relres_out) relres_out[v] = bb[v].x > 0.0 ? std::sqrt(std::max(r2[v], 0.0) / bb[v].x) : 0.0;
+    if (its[v] < 0) rc = std::isfinite(r2[v]) ? FAME_ERR_BREAKDOWN : FAME_ERR_NAN;
+    else if (act[v] && rc == FAME_OK) rc = FAME_ERR_NOT_CONVERGED;
+  }
+  if (rc != FAME_OK)
+    fail(&P, rc, rc == FAME_ERR_NOT_CONVERGED ? "pcg: not converged within maxit" : "pcg: breakdown or NaN");
+  return rc;
+}
+
+template int pcg_batched<float>(Plan&, const float2*, float2*, int, const int*, double, int, int*, double*,
+                                const unsigned char*);
+template int pcg_batched<double>(Plan&, const double2*, double2*, int, const int*, double, int, int*, double*,
+                                 const unsigned char*);
+
+int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, const int* d_inst, double tol,
+                  int max_rounds, double inner_tol32, int maxit32, const unsigned char* h_mask, long long* cg_iters,
+                  long long* b64_applies) {
+  if (nvec <= 0) return FAME_OK;
+  cudaStream_t st = P.stream;
+  const long long L = 4 * P.Nq;
+  cudaError_t e;
+  float2* res32 = (float2*)workspace(P, WS_MIX_B32, sizeof(float2) * L * nvec, &e);
+  FAME_CK(e, "mixed workspace");
+  float2* d32 = (float2*)workspace(P, WS_MIX_X32, sizeof(float2) * L * nvec, &e);
+  FAME_CK(e, "mixed workspace");
+  double2* res = (double2*)workspace(P, WS_MIX_RES, sizeof(double2) * L * nvec, &e);
+  FAME_CK(e, "mixed workspace");
+  const int nblk = dot_blocks(L, nvec);
+  char* sc = (char*)workspace(P, WS_MIX_MASK, (sizeof(int) + sizeof(double2)) * nvec + sizeof(double2) * nblk * nvec + 64, &e);
+  FAME_CK(e, "mixed workspace");
+  double2* dot = (double2*)sc;
+  double2* part = dot + nvec;
+  int* dmask = (int*)(part + (size_t)nblk * nvec);
+  FAME_CK(ensure_work(P, nvec), "mixed scratch");
+
+  std::vector<unsigned char> m(nvec, 1);
+  if (h_mask)
+    for (int v = 0; v < nvec; ++v) m[v] = h_mask[v] ? 1 : 0;
+  std::vector<int> mi(nvec);
+  for (int v = 0; v < nvec; ++v) mi[v] = m[v];
+  FAME_CK(cudaMemcpyAsync(dmask, mi.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "mixed init");
+  FAME_CK(dot_batched<double>(b, L, 0, 1, b, L, L, nvec, dot, part, nblk, dmask, st), "mixed dot");
+  std::vector<double2> bb(nvec);
+  FAME_CK(cudaMemcpyAsync(bb.data(), dot, sizeof(double2) * nvec, cudaMemcpyDeviceToHost, st), "mixed init");
+  FAME_CK(cudaStreamSynchronize(st), "mixed init");
+  for (int v = 0; v < nvec; ++v) {
+    if (!m[v]) continue;
+    FAME_CK(cudaMemsetAsync(x + (size_t)v * L, 0, sizeof(double2) * L, st), "mixed init");
+    FAME_CK(cudaMemsetAsync(Bx + (size_t)v * L, 0, sizeof(double2) * L, st), "mixed init");
+    if (!(bb[v].x > 0.0)) m[v] = 0;
+  }
+  // res = b (FP64) and its complex64 copy
+  FAME_CK(residual(b, Bx, res, res32, L, nvec, dmask, st), "mixed residual");
+  for (int v = 0; v < nvec; ++v) mi[v] = m[v];
+  FAME_CK(cudaMemcpyAsync(dmask, mi.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "mixed init");
+  int rc = FAME_OK;
+  std::vector<int> its(nvec);
+  VecCtx ctx;
+  ctx.inst = d_inst;
+  ctx.active = dmask;
+  ctx.nk = P.nk;
+  for (int round = 0; round < max_rounds; ++round) {
+    if (!std::any_of(m.begin(), m.end(), [](unsigned char a) { return a != 0; })) break;
+    int prc = pcg_batched<float>(P, res32, d32, nvec, d_inst, inner_tol32, maxit32, its.data(), nullptr, m.data());
+    if (prc == FAME_ERR_NAN || prc == FAME_ERR_BREAKDOWN) return prc;
+    for (int v = 0; v < nvec; ++v)
+      if (m[v] && cg_iters) *cg_iters += std::abs(its[v]);
+    FAME_CK(refine_acc(x, d32, L, nvec, dmask, st), "mixed acc");
+    double2* w0 = (double2*)P.d_work;
+    double2* w1 = w0 + (size_t)nvec * 6 * P.Nq;
+    FAME_CK(launch_fncB<double>(P, x, Bx, nvec, ctx, w0, w1, st), "mixed fncB");
+    if (b64_applies)
+      for (int v = 0; v < nvec; ++v) *b64_applies += m[v];
+    FAME_CK(residual(b, Bx, res, res32, L, nvec, dmask, st), "mixed residual");
+    FAME_CK(dot_batched<double>(res, L, 0, 1, res, L, L, nvec, dot, part, nblk, dmask, st), "mixed dot");
+    std::vector<double2> rr(nvec);
+    FAME_CK(cudaMemcpyAsync(rr.data(), dot, sizeof(double2) * nvec, cudaMemcpyDeviceToHost, st), "mixed check");
+    FAME_CK(cudaStreamSynchronize(st), "mixed check");
+    for (int v = 0; v < nvec; ++v) {
+      if (!m[v]) continue;
+      if (!std::isfinite(rr[v].x)) return fail(&P, FAME_ERR_NAN, "mixed solve: non-finite residual");
+      if (rr[v].x <= tol * tol * bb[v].x) m[v] = 0;
+    }
+    for (int v = 0; v < nvec; ++v) mi[v] = m[v];
+    FAME_CK(cudaMemcpyAsync(dmask, mi.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "mixed mask");
+  }
+  if (std::any_of(m.begin(), m.end(), [](unsigned char a) { return a != 0; })) rc = FAME_ERR_NOT_CONVERGED;
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Thick-restart Lanczos (fun_Lanczos/Lanczos.m), all selected instances in
+// lock step.  B*Q is cached column by column, so the reorthogonalisation of
+// Lanczos.m:63,66,69,159-167 needs no extra B applies; it runs as two passes
+// of classical Gram-Schmidt in the B inner product.
+// ---------------------------------------------------------------------------
+struct LzInst {
+  int inst = 0;
+  int k0 = 0, k = 0, sizeV = 1, j = 1, mm = 1;
+  bool justRestarted = false, done = false;
+  std::vector<double> Alpha, Beta, d, c;
+  double beta = 0.0;
+  std::vector<double> U;  // final Ritz combination, p x k0 column-major
+  long long steps = 0, restarts = 0, bapplies = 0, cgits = 0;
+};
+
+int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double tol, int maxit, int p,
+                const double* v0_host, double inner_tol, double* ew, double2* ev, double* res, long long* stats) {
+  const int na = (int)insts.size();
+  if (na == 0) return FAME_OK;
+  if (k0 < 1 || p <= k0 || p > 64 || maxit < 1 || !(tol > 0.0))
+    return fail(&P, FAME_ERR_BAD_ARG, "lanczos: need 1 <= k < p <= 64, maxit >= 1, tol > 0");
+  const long long L = 4 * P.Nq;
+  if (p > L) return fail(&P, FAME_ERR_BAD_ARG, "lanczos: p exceeds the vector length");
+  cudaStream_t st = P.stream;
+  cudaError_t e;
+  const double itol = inner_tol > 0 ? inner_tol : 1e-12;
+  const size_t cb = sizeof(double2) * L;
+  double2* Q = (double2*)workspace(P, WS_LZ_Q, cb * p * na, &e);
+  FAME_CK(e, "lanczos workspace Q");
+  double2* BQ = (double2*)workspace(P, WS_LZ_BQ, cb * p * na, &e);
+  FAME_CK(e, "lanczos workspace BQ");
+  double2* vec = (double2*)workspace(P, WS_LZ_VEC, cb * 7 * na, &e);
+  FAME_CK(e, "lanczos workspace");
+  double2* V = vec;               // current Lanczos vector v
+  double2* BV = V + L * na;       // B v
+  double2* AQ = BV + L * na;      // A q
+  double2* PR = AQ + L * na;      // B^{-1} A q   -> r
+  double2* BPR = PR + L * na;     // B * pr       -> B r
+  double2* T1 = BPR + L * na;     // scratch
+  double2* T2 = T1 + L * na;      // scratch
+  double2* TMP = (double2*)workspace(P, WS_LZ_TMP, cb * p, &e);
+  FAME_CK(e, "lanczos workspace");
+  int* dinst = (int*)workspace(P, WS_LZ_INST, sizeof(int) * na * 2 + 64, &e);
+  FAME_CK(e, "lanczos workspace");
+  int* dmask = dinst + na;
+  double2* coef = (double2*)workspace(P, WS_LZ_COEF, sizeof(double2) * 128 * na, &e);
+  FAME_CK(e, "lanczos workspace");
+  double* dU = (double*)workspace(P, WS_LZ_U, sizeof(double) * p * p, &e);
+  FAME_CK(e, "lanczos workspace");
+  double* dsc = (double*)workspace(P, WS_LZ_SCAL, sizeof(double) * na * 2 + 64, &e);
+  FAME_CK(e, "lanczos workspace");
+  double2* ddot = (double2*)workspace(P, WS_LZ_DOT, sizeof(double2) * na * 2 * 64, &e);
+  FAME_CK(e, "lanczos workspace");
+  const int nblk1 = dot_blocks(L, 1);
+  const int nblkb = dot_blocks(L, na);
+  double2* part = (double2*)workspace(P, WS_LZ_PART, sizeof(double2) * std::max(nblk1 * 64, nblkb * na) + 64, &e);
+  FAME_CK(e, "lanczos workspace");
+  FAME_CK(ensure_work(P, na), "lanczos scratch");
+  FAME_CK(cudaMemcpyAsync(dinst, insts.data(), sizeof(int) * na, cudaMemcpyHostToDevice, st), "lanczos init");
+
+  std::vector<LzInst> S(na);
+  for (int a = 0; a < na; ++a) {
+    S[a].inst = insts[a];
+    S[a].k0 = S[a].k = k0;
+  }
+  std::vector<int> mask(na, 1);
+  auto upload_mask = [&]() -> cudaError_t {
+    return cudaMemcpyAsync(dmask, mask.data(), sizeof(int) * na, cudaMemcpyHostToDevice, st);
+  };
+  FAME_CK(upload_mask(), "lanczos init");
+  VecCtx ctx;
+  ctx.inst = dinst;
+  ctx.active = dmask;
+  ctx.nk = P.nk;
+  auto fncB64 = [&](const double2* x, double2* y) {
+    double2* W0 = (double2*)P.d_work;
+    return launch_fncB<double>(P, x, y, na, ctx, W0, W0 + (size_t)na * 6 * P.Nq, st);
+  };
+  auto batched_dot = [&](const double2* a, const double2* b, std::vector<double2>& out) -> int {
+    FAME_CK(dot_batched<double>(a, L, 0, 1, b, L, L, na, ddot, part, nblkb, dmask, st), "lanczos dot");
+    out.resize(na);
+    FAME_CK(cudaMemcpyAsync(out.data(), ddot, sizeof(double2) * na, cudaMemcpyDeviceToHost, st), "lanczos dot");
+    FAME_CK(cudaStreamSynchronize(st), "lanczos dot");
+    return FAME_OK;
+  };
+  auto scale_vecs = [&](const double2* x, double2* y, const std::vector<double>& s) -> int {
+    FAME_CK(cudaMemcpyAsync(dsc, s.data(), sizeof(double) * na, cudaMemcpyHostToDevice, st), "lanczos scale");
+    FAME_CK(scale_batched<double>(x, y, L, na, dsc, dmask, st), "lanczos scale");
+    return FAME_OK;
+  };
+  // r -= sum_i c_i X_i (and the same on BX when given), c on device
+  auto project_out = [&](int a, double2* r, double2* br, int col0, int m) -> int {
+    double2* Qa = Q + (size_t)a * p * L;
+    double2* BQa = BQ + (size_t)a * p * L;
+    double2* ca = coef + (size_t)a * 128;
+    FAME_CK(dot_batched<double>(BQa + (size_t)col0 * L, 0, L, m, r, 0, L, 1, ca, part, nblk1, nullptr, st),
+            "lanczos gs dot");
+    FAME_CK(sub_combo<double>(r, Qa + (size_t)col0 * L, L, L, m, ca, st), "lanczos gs");
+    if (br) FAME_CK(sub_combo<double>(br, BQa + (size_t)col0 * L, L, L, m, ca, st), "lanczos gs");
+    return FAME_OK;
+  };
+  auto sub_host = [&](int a, double2* r, double2* br, int col0, std::vector<double2> cs) -> int {
+    double2* Qa = Q + (size_t)a * p * L;
+    double2* BQa = BQ + (size_t)a * p * L;
+    double2* ca = coef + (size_t)a * 128 + 64;
+    FAME_CK(cudaMemcpyAsync(ca, cs.data(), sizeof(double2) * cs.size(), cudaMemcpyHostToDevice, st), "lanczos");
+    FAME_CK(sub_combo<double>(r, Qa + (size_t)col0 * L, L, L, (int)cs.size(), ca, st), "lanczos");
+    if (br) FAME_CK(sub_combo<double>(br, BQa + (size_t)col0 * L, L, L, (int)cs.size(), ca, st), "lanczos");
+    // keep cs alive until the copy has been consumed
+    FAME_CK(cudaStreamSynchronize(st), "lanczos");
+    return FAME_OK;
+  };
+  const bool mixed = prec == FAME_C64;
+  long long total_b = 0;
+
+  // v0 (Lanczos.m:8; band_structure...:78-80): ones, or the caller's vector
+  {
+    std::vector<double2> hv(L);
+    for (long long i = 0; i < L; ++i) hv[i] = v0_host ? make_double2(v0_host[2 * i], v0_host[2 * i + 1]) : make_double2(1.0, 0.0);
+    for (int a = 0; a < na; ++a)
+      FAME_CK(cudaMemcpyAsync(V + (size_t)a * L, hv.data(), cb, cudaMemcpyHostToDevice, st), "lanczos v0");
+    FAME_CK(fncB64(V, BV), "lanczos v0");
+    total_b += na;
+    std::vector<double2> vb;
+    int rc = batched_dot(V, BV, vb);
+    if (rc) return rc;
+    std::vector<double> s(na);
+    for (int a = 0; a < na; ++a) s[a] = 1.0 / std::sqrt(std::fabs(vb[a].x));
+    if ((rc = scale_vecs(V, V, s))) return rc;
+    if ((rc = scale_vecs(BV, BV, s))) return rc;
+  }
+  const double eps = 2.2204e-16;  // Lanczos.m:23
+  int rc_final = FAME_OK;
+  std::vector<unsigned char> hm(na);
+  while (true) {
+    bool any = false;
+    for (int a = 0; a < na; ++a) {
+      mask[a] = S[a].done ? 0 : 1;
+      any |= !S[a].done;
+    }
+    if (!any) break;
+    FAME_CK(upload_mask(), "lanczos mask");
+    // Q(:, j) = v ; BQ(:, j) = B v
+    for (int a = 0; a < na; ++a) {
+      if (S[a].done) continue;
+      const int j = S[a].j - 1;
+      FAME_CK(cudaMemcpyAsync(Q + ((size_t)a * p + j) * L, V + (size_t)a * L, cb, cudaMemcpyDeviceToDevice, st), "lz");
+      FAME_CK(cudaMemcpyAsync(BQ + ((size_t)a * p + j) * L, BV + (size_t)a * L, cb, cudaMemcpyDeviceToDevice, st), "lz");
+    }
+    // r = fncA(q); alpha = real(r'*q)   (Lanczos.m:50-51)
+    FAME_CK(launch_fncA<double>(P, V, AQ, na, ctx, st), "lanczos fncA");
+    std::vector<double2> al;
+    int rc = batched_dot(AQ, V, al);
+    if (rc) return rc;
+    // pr = fncBinv(r)   (Lanczos.m:54,57,61)
+    for (int a = 0; a < na; ++a) hm[a] = mask[a];
+    if (mixed) {
+      long long cgi = 0, b64 = 0;
+      rc = solve_B_mixed(P, AQ, PR, BPR, na, dinst, itol, 6, 1e-6, 2000, hm.data(), &cgi, &b64);
+      if (rc == FAME_ERR_NAN || rc == FAME_ERR_BREAKDOWN) return rc;
+      total_b += b64;
+      for (int a = 0; a < na; ++a)
+        if (mask[a]) S[a].cgits += cgi / std::max(1, (int)std::count(mask.begin(), mask.end(), 1));
+    } else {
+      std::vector<int> its(na, 0);
+      rc = pcg_batched<double>(P, AQ, PR, na, dinst, itol, 10000, its.data(), nullptr, hm.data());
+      if (rc == FAME_ERR_NAN || rc == FAME_ERR_BREAKDOWN) return rc;
+      for (int a = 0; a < na; ++a)
+        if (mask[a]) {
+          S[a].cgits += std::abs(its[a]);
+          total_b += std::abs(its[a]);
+        }
+    }
+    // orthogonalisation (Lanczos.m:53-69)
+    for (int a = 0; a < na; ++a) {
+      if (S[a].done) continue;
+      LzInst& I = S[a];
+      const int j = I.j - 1;
+      const double alpha = al[a].x;
+      I.Alpha.push_back(alpha);
+      double2* r = PR + (size_t)a * L;
+      double2* br = mixed ? BPR + (size_t)a * L : nullptr;
+      if (I.j == 1) {
+        if ((rc = sub_host(a, r, br, j, {make_double2(alpha, 0.0)}))) return rc;
+      } else if (I.justRestarted) {
+        if ((rc = project_out(a, r, br, 0, I.j))) return rc;
+        I.justRestarted = false;
+      } else {
+        if ((rc = sub_host(a, r, br, j - 1, {make_double2(I.beta, 0.0), make_double2(alpha, 0.0)}))) return rc;
+        if ((rc = project_out(a, r, br, j - 1, 1))) return rc;  // :63
+      }
+      if ((rc = project_out(a, r, br, j, 1))) return rc;  // :66
+      if ((rc = project_out(a, r, br, 0, I.j))) return rc;  // :69 (two passes)
+      if ((rc = project_out(a, r, br, 0, I.j))) return rc;
+      I.steps++;
+    }
+    // rr = fncB(r); beta = sqrt(r'*rr); v = r/beta  (Lanczos.m:72-74)
+    if (!mixed) {
+      FAME_CK(fncB64(PR, BPR), "lanczos fncB");
+      for (int a = 0; a < na; ++a) total_b += mask[a];
+    }
+    std::vector<double2> rr;
+    if ((rc = batched_dot(PR, BPR, rr))) return rc;
+    std::vector<double> s(na, 0.0);
+    for (int a = 0; a < na; ++a) {
+      if (S[a].done) continue;
+      const double b2 = rr[a].x;
+      if (!std::isfinite(b2)) return fail(&P, FAME_ERR_NAN, "lanczos: non-finite beta");
+      S[a].beta = std::sqrt(std::fabs(b2));
+      if (!(S[a].beta > 0.0)) return fail(&P, FAME_ERR_BREAKDOWN, "lanczos: zero beta (invariant subspace)");
+      S[a].Beta.push_back(S[a].beta);
+      s[a] = 1.0 / S[a].beta;
+    }
+    if ((rc = scale_vecs(PR, V, s))) return rc;
+    if ((rc = scale_vecs(BPR, BV, s))) return rc;
+    // cycle ends
+    for (int a = 0; a < na; ++a) {
+      if (S[a].done) continue;
+      LzInst& I = S[a];
+      I.j++;
+      if (I.j <= p) continue;
+      // H = blkdiag(diag(d), tridiag(Alpha, Beta)) with arrowhead c (Lanczos.m:93-98)
+      const int kd = (int)I.d.size();
+      const int m1 = (int)I.Alpha.size();
+      const int np = kd + m1;
+      std::vector<double> H((size_t)np * np, 0.0);
+      for (int i = 0; i < kd; ++i) H[(size_t)i * np + i] = I.d[i];
+      for (int i = 0; i < m1; ++i) {
+        H[(size_t)(kd + i) * np + kd + i] = I.Alpha[i];
+        if (i + 1 < m1) {
+          H[(size_t)(kd + i) * np + kd + i + 1] = I.Beta[i];
+          H[(size_t)(kd + i + 1) * np + kd + i] = I.Beta[i];
+        }
+      }
+      for (int i = 0; i < kd; ++i) {
+        H[(size_t)i * np + kd] = I.c[i];
+        H[(size_t)kd * np + i] = I.c[i];
+      }
+      I.Alpha.clear();
+      I.Beta.clear();
+      std::vector<double> w, Uv;
+      jacobi_eig(H, np, w, Uv);
+      std::vector<int> ind(np);
+      std::iota(ind.begin(), ind.end(), 0);
+      std::stable_sort(ind.begin(), ind.end(), [&](int x, int y) { return w[x] > w[y]; });  // :109
+      int nconv = 0;
+      for (int i = 0; i < I.k0; ++i) {
+        const double resi = std::fabs(I.beta * Uv[(size_t)ind[i] * np + np - 1]);  // :106
+        if (resi < tol * std::max(std::pow(eps, 2.0 / 3.0), std::fabs(w[ind[i]]))) nconv++;  // :114
+      }
+      if (nconv >= I.k0 || I.mm == maxit) {  // :117
+        if (nconv < I.k0) rc_final = FAME_ERR_NOT_CONVERGED;
+        I.d.resize(I.k0);
+        I.U.assign((size_t)np * I.k0, 0.0);
+        for (int c2 = 0; c2 < I.k0; ++c2) {
+          I.d[c2] = w[ind[c2]];
+          for (int i = 0; i < np; ++i) I.U[(size_t)c2 * np + i] = Uv[(size_t)ind[c2] * np + i];
+        }
+        I.done = true;
+        continue;
+      }
+      int k = I.k0 + std::min(nconv, (p - I.k0) / 2);  // :122
+      if (k == 1 && p > 3) k = p / 2;
+      std::vector<double> Uk((size_t)np * k);
+      I.d.assign(k, 0.0);
+      I.c.assign(k, 0.0);
+      for (int c2 = 0; c2 < k; ++c2) {
+        I.d[c2] = w[ind[c2]];
+        for (int i = 0; i < np; ++i) Uk[(size_t)c2 * np + i] = Uv[(size_t)ind[c2] * np + i];
+        I.c[c2] = I.beta * Uk[(size_t)c2 * np + np - 1];  // :140
+      }
+      // Q(:,1:k) = Q*U ; BQ likewise (Lanczos.m:135-137)
+      FAME_CK(cudaMemcpyAsync(dU, Uk.data(), sizeof(double) * Uk.size(), cudaMemcpyHostToDevice, st), "lz restart");
+      double2* Qa = Q + (size_t)a * p * L;
+      double2* BQa = BQ + (size_t)a * p * L;
+      FAME_CK(block_rot<double>(Qa, TMP, L, L, np, k, dU, st), "lz restart");
+      FAME_CK(cudaMemcpyAsync(Qa, TMP, cb * k, cudaMemcpyDeviceToDevice, st), "lz restart");
+      FAME_CK(block_rot<double>(BQa, TMP, L, L, np, k, dU, st), "lz restart");
+      FAME_CK(cudaMemcpyAsync(BQa, TMP, cb * k, cudaMemcpyDeviceToDevice, st), "lz restart");
+      FAME_CK(cudaStreamSynchronize(st), "lz restart");
+      I.k = k;
+      I.justRestarted = true;
+      I.sizeV = k + 1;
+      I.j = k + 1;
+      I.mm++;
+      I.restarts++;
+    }
+  }
+  // Ritz vectors ev = Q*U(:, ind(1:k0)) (Lanczos.m:146-152) and outputs
+  double2* EV = ev;
+  for (int a = 0; a < na; ++a) {
+    LzInst& I = S[a];
+    for (int i = 0; i < k0; ++i) ew[(size_t)a * k0 + i] = I.d[i];
+    if (stats) {
+      stats[a * 4 + 0] = I.steps;
+      stats[a * 4 + 1] = I.restarts;
+      stats[a * 4 + 2] = 0;
+      stats[a * 4 + 3] = I.cgits;
+    }
+  }
+  if (stats)
+    for (int a = 0; a < na; ++a) stats[a * 4 + 2] = total_b / na;
+  if (EV || res) {
+    // one instance at a time through TMP (p columns available)
+    for (int a = 0; a < na; ++a) {
+      LzInst& I = S[a];
+      const int np = (int)(I.U.size() / k0);
+      FAME_CK(cudaMemcpyAsync(dU, I.U.data(), sizeof(double) * I.U.size(), cudaMemcpyHostToDevice, st), "lz ritz");
+      FAME_CK(block_rot<double>(Q + (size_t)a * p * L, TMP, L, L, np, k0, dU, st), "lz ritz");
+      if (EV) FAME_CK(cudaMemcpyAsync(EV + (size_t)a * k0 * L, TMP, cb * k0, cudaMemcpyDeviceToDevice, st), "lz ritz");
+      if (res) {
+        // ||A x - lambda B x|| / ||x|| in FP64 for each Ritz pair
+        VecCtx c1;
+        c1.nk = P.nk;
+        std::vector<int> ii(k0, I.inst);
+        int* di = (int*)workspace(P, WS_LZ_INST + 50, sizeof(int) * k0, &e);
+        FAME_CK(e, "lz res");
+        FAME_CK(cudaMemcpyAsync(di, ii.data(), sizeof(int) * k0, cudaMemcpyHostToDevice, st), "lz res");
+        c1.inst = di;
+        double2* AX = (double2*)workspace(P, WS_LZ_INST + 51, cb * k0, &e);
+        FAME_CK(e, "lz res");
+        double2* BX = (double2*)workspace(P, WS_LZ_INST + 52, cb * k0, &e);
+        FAME_CK(e, "lz res");
+        FAME_CK(ensure_work(P, k0), "lz res");
+        double2* w0 = (double2*)P.d_work;
+        double2* w1 = w0 + (size_t)k0 * 6 * P.Nq;
+        FAME_CK(launch_fncA<double>(P, TMP, AX, k0, c1, st), "lz res");
+        FAME_CK(launch_fncB<double>(P, TMP, BX, k0, c1, w0, w1, st), "lz res");
+        std::vector<double2> cl(k0), cb0(k0);
+        for (int i = 0; i < k0; ++i) {
+          cl[i] = make_double2(I.d[i], 0.0);
+          cb0[i] = make_double2(-1.0, 0.0);
+        }
+        // AX <- AX - lambda BX
+        double2* al2 = (double2*)workspace(P, WS_LZ_INST + 53, sizeof(double2) * 2 * k0, &e);
+        FAME_CK(e, "lz res");
+        std::vector<double2> ms(k0);
+        for (int i = 0; i < k0; ++i) ms[i] = make_double2(-I.d[i], 0.0);
+        std::vector<double2> ones(k0, make_double2(1.0, 0.0));
+        FAME_CK(cudaMemcpyAsync(al2, ms.data(), sizeof(double2) * k0, cudaMemcpyHostToDevice, st), "lz res");
+        FAME_CK(cudaMemcpyAsync(al2 + k0, ones.data(), sizeof(double2) * k0, cudaMemcpyHostToDevice, st), "lz res");
+        FAME_CK(axpby_batched<double>(BX, AX, L, L, k0, al2, al2 + k0, nullptr, st), "lz res");
+        const int nb = dot_blocks(L, k0);
+        double2* pp = (double2*)workspace(P, WS_LZ_INST + 54, sizeof(double2) * (nb * k0 + 2 * k0) + 64, &e);
+        FAME_CK(e, "lz res");
+        double2* o1 = pp + (size_t)nb * k0;
+        FAME_CK(dot_batched<double>(AX, L, 0, 1, AX, L, L, k0, o1, pp, nb, nullptr, st), "lz res");
+        FAME_CK(dot_batched<double>(TMP, L, 0, 1, TMP, L, L, k0, o1 + k0, pp, nb, nullptr, st), "lz res");
+        std::vector<double2> h2(2 * k0);
+        FAME_CK(cudaMemcpyAsync(h2.data(), o1, sizeof(double2) * 2 * k0, cudaMemcpyDeviceToHost, st), "lz res");
+        FAME_CK(cudaStreamSynchronize(st), "lz res");
+        for (int i = 0; i < k0; ++i) res[(size_t)a * k0 + i] = std::sqrt(h2[i].x / h2[k0 + i].x);
+      }
+    }
+    FAME_CK(cudaStreamSynchronize(st), "lz out");
+  }
+  if (rc_final != FAME_OK) fail(&P, rc_final, "lanczos: maxit restarts reached before tol");
+  return rc_final;
+}
+
+}  // namespace fame
+
+using namespace fame;
+
+
+extern "C" int fame_lanczos(fame_plan_t h, int prec, int inst, int k, double tol, int maxit, int p, const double* v0,
+                            double inner_tol, double* ew, void* ev, double* res, long long* stats) {
+  if (!h || !ew) return FAME_ERR_BAD_ARG;
+  Plan& P = h->P;
+  if (inst < 0 || inst >= P.nk) return fail(&P, FAME_ERR_BAD_ARG, "fame_lanczos: bad instance");
+  if (prec != FAME_C128 && prec != FAME_C64) return fail(&P, FAME_ERR_BAD_ARG, "fame_lanczos: bad precision");
+  std::vector<int> insts{inst};
+  return lanczos_run(P, prec, insts, k, tol, maxit, p, v0, inner_tol, ew, (double2*)ev, res, stats);
+}
+
+extern "C" int fame_band_solve(fame_plan_t h, int prec, int k, double tol, int maxit, int p, double inner_tol,
+                               double* ew, double* res, long long* stats) {
+  if (!h || !ew) return FAME_ERR_BAD_ARG;
+  Plan& P = h->P;
+  if (prec != FAME_C128 && prec != FAME_C64) return fail(&P, FAME_ERR_BAD_ARG, "fame_band_solve: bad precision");
+  std::vector<int> insts(P.nk);
+  std::iota(insts.begin(), insts.end(), 0);
+  return lanczos_run(P, prec, insts, k, tol, maxit, p, nullptr, inner_tol, ew, nullptr, res, stats);
+}

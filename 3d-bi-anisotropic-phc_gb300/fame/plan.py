@@ -1,0 +1,226 @@
+"""Python view of a FAME plan: one cubic n^3 grid, ``nk`` k-point instances.
+
+Vectors are torch tensors on the CUDA device (complex128 -> the FP64 path,
+complex64 -> the complex64 path) of shape (nvec, L) or (L,), or NumPy arrays
+on the host (staged by the library).  Calls run on torch's current CUDA
+stream.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import check, load
+from .setup import covariant_blocks
+
+try:
+    import torch
+except ImportError:  # pragma: no cover - torch is required on the GPU path
+    torch = None
+
+
+def _prec_of(x):
+    if torch is not None and isinstance(x, torch.Tensor):
+        if x.dtype == torch.complex128:
+            return L.FAME_C128
+        if x.dtype == torch.complex64:
+            return L.FAME_C64
+        raise TypeError(f"unsupported dtype {x.dtype}")
+    x = np.asarray(x)
+    if x.dtype == np.complex128:
+        return L.FAME_C128
+    if x.dtype == np.complex64:
+        return L.FAME_C64
+    raise TypeError(f"unsupported dtype {x.dtype}")
+
+
+class Plan:
+    """``fame_plan_create`` wrapper (replaces the per-k mtx_A / mtx_B / fnc setup)."""
+
+    def __init__(self, n: int, thetas, phase, tensors):
+        self._lib = load()
+        self.n = int(n)
+        th = np.ascontiguousarray(np.asarray(thetas, dtype=np.float64).reshape(-1, 3))
+        self.nk = th.shape[0]
+        self.thetas = th
+        ph = np.ascontiguousarray(np.asarray(phase, dtype=np.uint8).reshape(-1))
+        if ph.size != self.n ** 3:
+            raise ValueError("phase must hold n^3 vertex ids")
+        t = np.asarray(tensors, dtype=np.complex128)
+        if t.ndim == 2:
+            t = np.broadcast_to(t, (self.nk,) + t.shape)
+        t = np.ascontiguousarray(t.reshape(self.nk, -1, 27))
+        self.nphase = t.shape[1]
+        self.tensors = t
+        self.phase = ph
+        self._h = C.c_void_p()
+        pd = C.POINTER(C.c_double)
+        rc = self._lib.fame_plan_create(C.byref(self._h), self.n, self.nk, th.ctypes.data_as(pd),
+                                        ph.ctypes.data_as(C.POINTER(C.c_uint8)), self.nphase,
+                                        t.view(np.float64).ctypes.data_as(pd))
+        check(rc, None, "fame_plan_create")
+        self.Nq = self.n ** 3
+
+    @classmethod
+    def from_phases(cls, n, thetas, phase, constitutive_per_phase, A=None):
+        """Plan from per-phase 6x6 constitutive blocks (shared by all instances,
+        or one list per instance)."""
+        c = np.asarray(constitutive_per_phase, dtype=np.complex128)
+        if c.ndim == 3:
+            tens = np.stack([covariant_blocks(m, A) for m in c])
+        else:
+            tens = np.stack([np.stack([covariant_blocks(m, A) for m in ci]) for ci in c])
+        return cls(n, thetas, phase, tens)
+
+    # -- life cycle ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.fame_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _stream(self):
+        if torch is not None and torch.cuda.is_available():
+            self._lib.fame_set_stream(self._h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+
+    def sync(self):
+        check(self._lib.fame_sync(self._h), self._h, "fame_sync")
+
+    # -- generic call -------------------------------------------------------
+    def _call(self, fn, x, out_len, inst, *extra, name=""):
+        prec = _prec_of(x)
+        is_torch = torch is not None and isinstance(x, torch.Tensor)
+        single = x.ndim == 1
+        if is_torch:
+            xx = x.reshape(1, -1) if single else x
+            xx = xx.contiguous()
+            nvec = xx.shape[0]
+            y = torch.empty((nvec, out_len), dtype=xx.dtype, device=xx.device)
+            xp, yp, flags = C.c_void_p(xx.data_ptr()), C.c_void_p(y.data_ptr()), 0
+            self._stream()
+        else:
+            xx = np.ascontiguousarray(np.asarray(x).reshape(1, -1) if single else np.asarray(x))
+            nvec = xx.shape[0]
+            y = np.empty((nvec, out_len), dtype=xx.dtype)
+            xp, yp, flags = C.c_void_p(xx.ctypes.data), C.c_void_p(y.ctypes.data), L.FAME_HOST_PTR
+        ip = None
+        if inst is not None:
+            ia = np.ascontiguousarray(np.broadcast_to(np.asarray(inst, dtype=np.int32), (nvec,)))
+            ip = ia.ctypes.data_as(C.POINTER(C.c_int))
+        rc = fn(self._h, prec, *extra[:1], xp, yp, nvec, ip, *extra[1:], flags) if extra else \
+            fn(self._h, prec, xp, yp, nvec, ip, flags)
+        check(rc, self._h, name)
+        return y.reshape(-1) if single else y
+
+    # -- operator handles ---------------------------------------------------
+    def apply_A(self, x, inst=None):
+        """fncA (fun_Lanczos/fncA.m)."""
+        return self._call(self._lib.fame_apply_A, x, 4 * self.Nq, inst, name="fame_apply_A")
+
+    def apply_B(self, x, inst=None):
+        """fncB (fun_Lanczos/fncB.m)."""
+        return self._call(self._lib.fame_apply_B, x, 4 * self.Nq, inst, name="fame_apply_B")
+
+    def transform(self, x, trans: int, inst=None):
+        """MtxVecMul_FFT: trans 0 'notranspose', 1 'transpose' (3Nq vectors)."""
+        return self._call(self._lib.fame_curl_transform, x, 3 * self.Nq, inst, int(trans), name="fame_curl_transform")
+
+    def handle(self, which: int, x, inst=None):
+        """fnc.Pr / Qr / Prs / Qrs (Funhand_Generate_Lanzcos.m:79-82)."""
+        out = 3 * self.Nq if which in (L.FAME_PR, L.FAME_QR) else 2 * self.Nq
+        return self._call(self._lib.fame_apply_handle, x, out, inst, int(which), name="fame_apply_handle")
+
+    def material(self, x, inst=None):
+        """[M_int J_int'; J_int N_int] on 6Nq Bloch-frame vectors."""
+        return self._call(self._lib.fame_apply_material, x, 6 * self.Nq, inst, name="fame_apply_material")
+
+    def apply_Binv(self, x, tol=1e-12, maxit=10000, inst=None, raise_on_noconv=False):
+        """fncinvB: CG on B (fun_Lanczos/fncinvB.m).  Returns (y, iters, relres)."""
+        prec = _prec_of(x)
+        is_torch = torch is not None and isinstance(x, torch.Tensor)
+        single = x.ndim == 1
+        if is_torch:
+            xx = (x.reshape(1, -1) if single else x).contiguous()
+            nvec = xx.shape[0]
+            y = torch.empty_like(xx)
+            xp, yp, flags = C.c_void_p(xx.data_ptr()), C.c_void_p(y.data_ptr()), 0
+            self._stream()
+        else:
+            xx = np.ascontiguousarray(np.asarray(x).reshape(1, -1) if single else np.asarray(x))
+            nvec = xx.shape[0]
+            y = np.empty_like(xx)
+            xp, yp, flags = C.c_void_p(xx.ctypes.data), C.c_void_p(y.ctypes.data), L.FAME_HOST_PTR
+        its = np.zeros(nvec, dtype=np.int32)
+        rr = np.zeros(nvec, dtype=np.float64)
+        ip = None
+        if inst is not None:
+            ia = np.ascontiguousarray(np.broadcast_to(np.asarray(inst, dtype=np.int32), (nvec,)))
+            ip = ia.ctypes.data_as(C.POINTER(C.c_int))
+        rc = self._lib.fame_apply_Binv(self._h, prec, xp, yp, nvec, ip, float(tol), int(maxit),
+                                       its.ctypes.data_as(C.POINTER(C.c_int)),
+                                       rr.ctypes.data_as(C.POINTER(C.c_double)), flags)
+        if rc != L.FAME_OK and (rc != L.FAME_ERR_NOT_CONVERGED or raise_on_noconv):
+            check(rc, self._h, "fame_apply_Binv")
+        return (y.reshape(-1) if single else y), its, rr
+
+    # -- solvers ------------------------------------------------------------
+    def lanczos(self, k, tol=1e-10, maxit=10000, p=None, v0=None, inst=0, prec="c128", inner_tol=1e-12,
+                want_vectors=True):
+        """Thick-restart Lanczos (fun_Lanczos/Lanczos.m) on instance `inst`.
+
+        Returns dict(ew, omega, res, ev, stats, status)."""
+        p = 2 * k if p is None else p
+        ew = np.zeros(k, dtype=np.float64)
+        res = np.zeros(k, dtype=np.float64)
+        stats = np.zeros(4, dtype=np.int64)
+        pd = C.POINTER(C.c_double)
+        v0p = None
+        if v0 is not None:
+            v0a = np.ascontiguousarray(np.asarray(v0, dtype=np.complex128).reshape(-1))
+            v0p = v0a.view(np.float64).ctypes.data_as(pd)
+        ev = None
+        evp = None
+        if want_vectors:
+            ev = torch.empty((k, 4 * self.Nq), dtype=torch.complex128, device="cuda")
+            evp = C.c_void_p(ev.data_ptr())
+        self._stream()
+        pr = L.FAME_C64 if prec in ("c64", "mixed", L.FAME_C64) else L.FAME_C128
+        rc = self._lib.fame_lanczos(self._h, pr, int(inst), int(k), float(tol), int(maxit), int(p), v0p,
+                                    float(inner_tol), ew.ctypes.data_as(pd), evp, res.ctypes.data_as(pd),
+                                    stats.ctypes.data_as(C.POINTER(C.c_longlong)))
+        if rc not in (L.FAME_OK, L.FAME_ERR_NOT_CONVERGED):
+            check(rc, self._h, "fame_lanczos")
+        return dict(ew=ew, omega=1.0 / ew, res=res, ev=ev, stats=stats, status=rc)
+
+    def band_solve(self, k, tol=1e-10, maxit=10000, p=None, prec="c64", inner_tol=1e-12):
+        """All instances at once (fame_band_solve).  Returns dict(ew, omega, res, stats, status)."""
+        p = 2 * k if p is None else p
+        ew = np.zeros((self.nk, k), dtype=np.float64)
+        res = np.zeros((self.nk, k), dtype=np.float64)
+        stats = np.zeros((self.nk, 4), dtype=np.int64)
+        pd = C.POINTER(C.c_double)
+        self._stream()
+        pr = L.FAME_C64 if prec in ("c64", "mixed", L.FAME_C64) else L.FAME_C128
+        rc = self._lib.fame_band_solve(self._h, pr, int(k), float(tol), int(maxit), int(p), float(inner_tol),
+                                       ew.ctypes.data_as(pd), res.ctypes.data_as(pd),
+                                       stats.ctypes.data_as(C.POINTER(C.c_longlong)))
+        if rc not in (L.FAME_OK, L.FAME_ERR_NOT_CONVERGED):
+            check(rc, self._h, "fame_band_solve")
+        return dict(ew=ew, omega=1.0 / ew, res=res, stats=stats, status=rc)

@@ -1,0 +1,147 @@
+/*
+ * FAME GB300: C ABI of the nullspace-free FFT eigensolver hot path for the
+ * 3D bi-anisotropic Maxwell generalised eigenproblem on quasi-periodic grids.
+ *
+ * Every entry point replaces one MATLAB handle or function of the reference
+ * (FAME-GPU/3D-Bi-Anisotropic-PhC); the replaced interface is cited beside
+ * each declaration.  Conventions:
+ *   - vectors are interleaved complex (double2 for FAME_C128, float2 for
+ *     FAME_C64) in the reference's MATLAB order: x-fastest grids, blocks
+ *     stacked as in the reference ([x1; x2] halves, components 1,2,3);
+ *   - a plan holds `nk` k-point instances of one cubic n^3 grid; a call
+ *     processes `nvec` vectors, vector v belonging to instance inst[v]
+ *     (inst == NULL: instance v % nk);
+ *   - pointers are device pointers unless `flags` has FAME_HOST_PTR, in which
+ *     case the library stages them through device memory;
+ *   - calls are ordered on the plan's CUDA stream (fame_set_stream); a plan is
+ *     not thread-safe, distinct plans are;
+ *   - every call returns a fame_status; fame_last_error() describes failures.
+ */
+#ifndef FAME_GB300_H
+#define FAME_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fame_plan_s* fame_plan_t;
+
+enum fame_status {
+  FAME_OK = 0,
+  FAME_ERR_BAD_ARG = 1,
+  FAME_ERR_CUDA = 2,
+  FAME_ERR_NOT_CONVERGED = 3,
+  FAME_ERR_BREAKDOWN = 4,
+  FAME_ERR_NAN = 5,
+  FAME_ERR_UNSUPPORTED = 6,
+  FAME_ERR_SINGULAR = 7,
+  FAME_ERR_ALLOC = 8
+};
+
+enum fame_precision { FAME_C128 = 0, FAME_C64 = 1 };
+
+enum fame_handle { FAME_PR = 0, FAME_QR = 1, FAME_PRS = 2, FAME_QRS = 3 };
+
+#define FAME_HOST_PTR 1
+
+/* Library version string. */
+const char* fame_version(void);
+
+/*
+ * Create a plan for `nk` k-points of one n^3 grid.
+ *   theta   [nk*3]   Bloch angles theta_d = k . a_d per instance
+ *                    (band_structure_woodpile_Lanczos_n60_gamma0p2.m:54-56).
+ *   phase   [n^3]    phase id of every vertex, x fastest (host)
+ *                    (the inside index set of Material_Matrix_Generate_Mult_Point.m:15).
+ *   tensors [nk*nphase*27*2]  per instance and phase, the covariant N, M, J
+ *                    blocks (3x3 row-major each, interleaved complex), i.e. the
+ *                    A'*X*A blocks of the inverted 6x6 constitutive matrix that
+ *                    DistMaterialMatrix places (Material_Matrix_Generate_Mult_Point.m:28-31,38-48).
+ * Replaces the per-k setup SVD_Matrix_Generate.m:24-30,
+ * Interpolation_Material_Matrix_Mult_Point_vertex.m:1-28 and
+ * Funhand_Generate_Lanzcos.m:1-82 (handles closed over mtx_A / mtx_B).
+ */
+int fame_plan_create(fame_plan_t* plan, int n, int nk, const double* theta, const uint8_t* phase, int nphase,
+                     const double* tensors);
+int fame_plan_destroy(fame_plan_t plan);
+/* Use `stream` (a cudaStream_t) for all later calls on this plan. */
+int fame_set_stream(fame_plan_t plan, void* stream);
+int fame_sync(fame_plan_t plan);
+const char* fame_last_error(fame_plan_t plan);
+int fame_plan_info(fame_plan_t plan, int* n, int* nk, long long* nq);
+
+/* y = A x on 4*Nq vectors.  Replaces fun_Lanczos/fncA.m:1-5. */
+int fame_apply_A(fame_plan_t plan, int prec, const void* x, void* y, int nvec, const int* inst, int flags);
+
+/* y = B x on 4*Nq vectors.  Replaces fun_Lanczos/fncB.m:1-7 and
+ * fun_no_inv/fncB_Generate_no_inv.m:1-9. */
+int fame_apply_B(fame_plan_t plan, int prec, const void* x, void* y, int nvec, const int* inst, int flags);
+
+/* y = B^{-1} x by conjugate gradients to relative residual `tol` within
+ * `maxit` iterations per vector; iters/relres (may be NULL) receive per-vector
+ * results.  Returns FAME_ERR_NOT_CONVERGED if any vector missed `tol`.
+ * Replaces fun_Lanczos/fncinvB.m:1-5 (pcg(B_op, x, tol, maxit)). */
+int fame_apply_Binv(fame_plan_t plan, int prec, const void* x, void* y, int nvec, const int* inst, double tol,
+                    int maxit, int* iters, double* relres, int flags);
+
+/* Curl singular-vector transform on 3*Nq vectors: trans = 0 'notranspose'
+ * (S .* ifftn(.)*sqrt(N) per component), 1 'transpose' (fftn(conj(S).*.)/sqrt(N)).
+ * Replaces subroutines/MtxVecMul_FFT.m:1, gMtxVecMul_FFT.m:1 and
+ * kMtxVecMul_FFT.m:1 for quasi-periodic ('DFT') types. */
+int fame_curl_transform(fame_plan_t plan, int prec, int trans, const void* x, void* y, int nvec, const int* inst,
+                        int flags);
+
+/* Composed handles fnc.Pr / fnc.Qr (2Nq -> 3Nq) and fnc.Prs / fnc.Qrs
+ * (3Nq -> 2Nq).  Replaces fun_Lanczos/Funhand_Generate_Lanzcos.m:79-82. */
+int fame_apply_handle(fame_plan_t plan, int prec, int which, const void* x, void* y, int nvec, const int* inst,
+                      int flags);
+
+/* [u'; v'] = [M_int J_int^H; J_int N_int] [u; v] on 6*Nq vectors (the
+ * material middle factor of fncB, Bloch frame).  Replaces the sparse products
+ * mtx_B.M_int*u + mtx_B.J_int'*v, mtx_B.J_int*u + mtx_B.N_int*v of
+ * fun_Lanczos/fncB.m:4-5. */
+int fame_apply_material(fame_plan_t plan, int prec, const void* x, void* y, int nvec, const int* inst, int flags);
+
+/*
+ * Thick-restart Lanczos for the `k` largest eigenvalues of B^{-1}A of one
+ * instance, in the B inner product, restart size p, Ritz tolerance `tol`,
+ * at most `maxit` restarts.  v0 [4Nq] (host, complex128) or NULL for ones.
+ * Inner solves: B^{-1} by CG at `inner_tol` (<= 0: 1e-12).
+ * prec = FAME_C128: every matvec in complex128 (the reference's form).
+ * prec = FAME_C64 : complex64 matvecs and inner CG with FP64 recurrence,
+ *                   reorthogonalisation and a final FP64 refinement.
+ * Outputs: ew[k] eigenvalues of B^{-1}A, descending (omega = 1/ew);
+ * ev (device, complex128, 4Nq x k, may be NULL) B-normalised Ritz vectors;
+ * res[k] (may be NULL) ||B x - omega A x|| / ||B x|| with FP64 matvecs;
+ * stats[4] (may be NULL): Lanczos steps, restarts, B applies, inner CG iterations.
+ * Replaces fun_Lanczos/Lanczos.m:1-167 (with op_invB of
+ * band_structure_woodpile_Lanczos_n60_gamma0p2.m:74-81).
+ */
+int fame_lanczos(fame_plan_t plan, int prec, int inst, int k, double tol, int maxit, int p, const double* v0,
+                 double inner_tol, double* ew, void* ev, double* res, long long* stats);
+
+/*
+ * Batched band solve: fame_lanczos on every instance of the plan at once
+ * (vectors of all k-points advance together; converged k-points drop out).
+ * ew[nk*k], res[nk*k] (may be NULL), stats[nk*4] (may be NULL).
+ */
+int fame_band_solve(fame_plan_t plan, int prec, int k, double tol, int maxit, int p, double inner_tol,
+                    double* ew, double* res, long long* stats);
+
+/*
+ * Covariant material blocks of one phase: invert the 6x6 constitutive block
+ * [eps xi; zeta mu] (row-major, interleaved complex, 36*2 doubles), split it
+ * and return A'*X*A of the (1,1), (2,2) and (1,2) blocks as 27 complex
+ * (N | M | J, row-major) in out[54].  lattice: 3x3 row-major, columns are the
+ * primitive vectors.  Replaces Physical_settings_woodpile.m:91-96,184-194.
+ */
+int fame_material_blocks(const double* eps_xi_zeta_mu, const double* lattice, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FAME_GB300_H */
