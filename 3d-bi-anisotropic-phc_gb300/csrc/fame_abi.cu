@@ -30,6 +30,7 @@ template <> PlanData<double>& pdata_mut<double>(Plan& P) { return P.d64; }
 template <> PlanData<float>& pdata_mut<float>(Plan& P) { return P.d32; }
 
 static std::string g_static_error;
+unsigned long long g_kernel_launches = 0;
 
 void* workspace(Plan& P, int id, size_t bytes, cudaError_t* err) {
   *err = cudaSuccess;
@@ -45,6 +46,27 @@ void* workspace(Plan& P, int id, size_t bytes, cudaError_t* err) {
   if (*err != cudaSuccess) return nullptr;
   P.ws_size[id] = bytes;
   return P.ws_ptr[id];
+}
+
+constexpr size_t kRingBytes = 1 << 20;
+
+cudaError_t h2d_async(Plan& P, void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return cudaSuccess;
+  if (!P.h_ring) {
+    cudaError_t e = cudaMallocHost((void**)&P.h_ring, kRingBytes);
+    if (e != cudaSuccess) return e;
+    P.ring_pos = 0;
+  }
+  if (bytes > kRingBytes) return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+  if (P.ring_pos + bytes > kRingBytes) {  // wrap only once earlier copies have been consumed
+    cudaError_t e = cudaStreamSynchronize(P.stream);
+    if (e != cudaSuccess) return e;
+    P.ring_pos = 0;
+  }
+  char* slot = P.h_ring + P.ring_pos;
+  std::memcpy(slot, src, bytes);
+  P.ring_pos += (bytes + 255) & ~size_t(255);
+  return cudaMemcpyAsync(dst, slot, bytes, cudaMemcpyHostToDevice, P.stream);
 }
 
 void free_workspaces(Plan& P) {
@@ -146,6 +168,7 @@ template <class R> void free_tables(PlanData<R>& d) {
   cudaFree(d.tau);
   cudaFree(d.sxyz);
   cudaFree(d.mat);
+  cudaFree(d.pc);
   d = PlanData<R>();
 }
 
@@ -191,6 +214,8 @@ extern "C" {
 
 const char* fame_version(void) { return "fame-gb300 0.1 (sm_103a)"; }
 
+long long fame_kernel_launches(void) { return (long long)__atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED); }
+
 int fame_plan_create(fame_plan_t* out, int n, int nk, const double* theta, const uint8_t* phase, int nphase,
                      const double* tensors) {
   if (!out) return FAME_ERR_BAD_ARG;
@@ -224,6 +249,29 @@ int fame_plan_create(fame_plan_t* out, int n, int nk, const double* theta, const
       delete h;
       return FAME_ERR_BAD_ARG;
     }
+  // volume-averaged Herm(N) | Herm(M) | J per instance (CG preconditioner)
+  {
+    std::vector<double> frac(nphase, 0.0);
+    for (long long i = 0; i < P.Nq; ++i) frac[phase[i]] += 1.0;
+    for (double& f : frac) f /= double(P.Nq);
+    P.mat_avg.assign((size_t)nk * 54, 0.0);
+    for (int k = 0; k < nk; ++k)
+      for (int ph = 0; ph < nphase; ++ph) {
+        const double* src = &P.mat_host[((size_t)k * nphase + ph) * 54];
+        for (int blk = 0; blk < 3; ++blk)
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+              const int a = (blk * 9 + i * 3 + j) * 2, t = (blk * 9 + j * 3 + i) * 2;
+              double re = src[a], im = src[a + 1];
+              if (blk < 2) {  // Hermitian part of N and M
+                re = 0.5 * (re + src[t]);
+                im = 0.5 * (im - src[t + 1]);
+              }
+              P.mat_avg[(size_t)k * 54 + a] += frac[ph] * re;
+              P.mat_avg[(size_t)k * 54 + a + 1] += frac[ph] * im;
+            }
+      }
+  }
   int rc = check_singular(P);
   if (rc != FAME_OK) {
     g_static_error = P.last_error;
@@ -261,9 +309,27 @@ int fame_plan_destroy(fame_plan_t h) {
   cudaFree(P.d_inst);
   cudaFree(P.d_red);
   cudaFree(P.d_stage);
+  cudaFree(P.d_mat_avg);
+  if (P.h_ring) cudaFreeHost(P.h_ring);
   free_workspaces(P);
   delete h;
   return FAME_OK;
+}
+
+int fame_set_option(fame_plan_t h, int option, double value) {
+  if (!h) return FAME_ERR_BAD_ARG;
+  Plan& P = h->P;
+  switch (option) {
+    case FAME_OPT_PRECOND:
+      P.opt_precond = value != 0.0;
+      return FAME_OK;
+    case FAME_OPT_TOL32:
+      if (!(value > 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: tol32 in (0,1)");
+      P.opt_tol32 = value;
+      return FAME_OK;
+    default:
+      return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: unknown option");
+  }
 }
 
 int fame_set_stream(fame_plan_t h, void* stream) {

@@ -12,6 +12,10 @@
 
 namespace fame {
 
+// Number of kernels this library has launched (all plans, all threads).
+extern unsigned long long g_kernel_launches;
+#define FAME_LAUNCHED(n) __atomic_fetch_add(&::fame::g_kernel_launches, (unsigned long long)(n), __ATOMIC_RELAXED)
+
 // Which vectors of a batch belong to which k-point instance, and which are
 // still active (converged vectors of a batched solve are skipped).
 struct VecCtx {
@@ -28,6 +32,7 @@ template <class R> struct PlanData {
   cx<R>* tau = nullptr;  // [nk][3]   exp(i*theta_d/n): Bloch phase of one periodic shift
   cx<R>* sxyz = nullptr; // [nk][3n]  S_sDFT per axis (the MtxVecMul_FFT phase)
   cx<R>* mat = nullptr;  // [nk][nphase][27]: Herm(N) | Herm(M) | J, row-major 3x3 each
+  cx<R>* pc = nullptr;   // [nk][10][Nq] CG preconditioner: inverse 4x4 Hermitian blocks (lazy)
 };
 
 struct Plan {
@@ -37,7 +42,12 @@ struct Plan {
   int nphase = 0;
   int device = 0;
   cudaStream_t stream = nullptr;
+  // options (fame_set_option)
+  int opt_precond = 1;                // CG on B preconditioned by the averaged-medium B0^{-1}
+  double opt_tol32 = 1e-6;            // complex64 CG tolerance of the first refinement round
   std::vector<double> theta;          // [nk][3]
+  std::vector<double> mat_avg;        // [nk][27][2] volume-averaged Herm(N) | Herm(M) | J
+  double2* d_mat_avg = nullptr;       // device copy
   std::vector<double> mat_host;       // [nk][nphase][27][2] covariant N | M | J blocks
   uint8_t* d_phase = nullptr;         // [Nq] phase id per vertex
   PlanData<double> d64;
@@ -57,7 +67,14 @@ struct Plan {
   // named grow-only device workspaces of the solvers
   std::vector<void*> ws_ptr;
   std::vector<size_t> ws_size;
+  // pinned ring for small host->device uploads (a copy from pageable memory
+  // would synchronise the stream)
+  char* h_ring = nullptr;
+  size_t ring_pos = 0;
 };
+
+// Asynchronous small upload through the plan's pinned ring (stream-ordered).
+cudaError_t h2d_async(Plan& P, void* dst, const void* src, size_t bytes);
 
 // Workspace slot `id` of at least `bytes` bytes (contents not preserved on growth).
 void* workspace(Plan& P, int id, size_t bytes, cudaError_t* err);
@@ -87,6 +104,19 @@ cudaError_t launch_handle(const Plan& P, int which, const cx<R>* x, cx<R>* y, in
 template <class R>
 cudaError_t launch_material(const Plan& P, const cx<R>* uv, cx<R>* out, int nvec,
                             const VecCtx& ctx, cx<R>* w1, cudaStream_t st);
+
+// CG preconditioner M = B0^{-1}: B0 is fncB of the homogeneous medium with the
+// volume-averaged vertex tensors, block diagonal in the frequency basis
+// (one 4x4 Hermitian block per voxel).  Built once per plan and precision.
+template <class R> cudaError_t build_precond(Plan& P, cudaStream_t st);
+// z = M r per vector; partial sums (Re r'z, |r|^2) per block into partial.
+template <class R>
+cudaError_t precond_apply(const Plan& P, const cx<R>* r, cx<R>* z, int nvec, const VecCtx& ctx, double2* partial,
+                          int nblk, cudaStream_t st);
+// x += a p ; r -= a q ; z = M r ; partial (Re r'z, |r|^2)
+template <class R>
+cudaError_t pcg_update(const Plan& P, cx<R>* x, cx<R>* r, cx<R>* z, const cx<R>* p, const cx<R>* q, int nvec,
+                       const VecCtx& ctx, const double* alpha, double2* partial, int nblk, cudaStream_t st);
 
 bool n_supported(int n);
 

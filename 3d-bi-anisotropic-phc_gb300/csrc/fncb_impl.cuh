@@ -89,7 +89,7 @@ template <class R> __device__ __forceinline__ R rsqrt_n3(int n) {
 // S_x S_y when WITH_S.
 // ---------------------------------------------------------------------------
 template <class R, int N, bool PREP, bool WITH_S>
-__global__ void __launch_bounds__(3 * N < 32 ? 32 : 3 * N)
+__global__ void __launch_bounds__(((3 * N + 31) / 32) * 32)
 k_plane_inv(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d, VecCtx ctx,
             long long in_stride, long long in_side_stride, long long out_stride, int side0) {
   constexpr int LD = N + 1;
@@ -171,7 +171,7 @@ k_plane_inv(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d,
 // else copies the 3 components out.
 // ---------------------------------------------------------------------------
 template <class R, int N, bool POST, bool WITH_S>
-__global__ void __launch_bounds__(3 * N < 32 ? 32 : 3 * N)
+__global__ void __launch_bounds__(((3 * N + 31) / 32) * 32)
 k_plane_fwd(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, VecCtx ctx,
             long long w_stride, long long out_stride, long long out_side_stride, int side0) {
   constexpr int LD = N + 1;
@@ -285,6 +285,7 @@ cudaError_t plane_inv(const Plan& P, const PlanData<R>& d, const cx<R>* x, cx<R>
   auto kfn = k_plane_inv<R, N, PREP, WITH_S>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
+  FAME_LAUNCHED(1);
   kfn<<<dim3(N, nside, nvec), threads, sm, st>>>(x, out, d, ctx, in_stride, in_side_stride, out_stride,
                                                  side0);
   return cudaGetLastError();
@@ -299,6 +300,7 @@ cudaError_t plane_fwd(const Plan& P, const PlanData<R>& d, const cx<R>* w, cx<R>
   auto kfn = k_plane_fwd<R, N, POST, WITH_S>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
+  FAME_LAUNCHED(1);
   kfn<<<dim3(N, nside, nvec), threads, sm, st>>>(w, y, d, ctx, w_stride, out_stride, out_side_stride,
                                                  side0);
   return cudaGetLastError();
@@ -308,6 +310,7 @@ template <class R, int N, int DIR, int SMODE>
 cudaError_t col(const PlanData<R>& d, cx<R>* w, int nfield, int nvec, long long stride, const VecCtx& ctx,
                 cudaStream_t st) {
   dim3 g((N * N + 127) / 128, nfield, nvec);
+  FAME_LAUNCHED(1);
   k_col<R, N, DIR, SMODE><<<g, 128, 0, st>>>(w, d, ctx, stride);
   return cudaGetLastError();
 }

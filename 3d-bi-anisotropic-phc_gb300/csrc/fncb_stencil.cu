@@ -178,9 +178,11 @@ template <class R>
 cudaError_t stencil(const Plan& P, cx<R>* w0, cx<R>* w1, int nvec, const VecCtx& ctx, cudaStream_t st) {
   const PlanData<R>& d = pdata<R>(P);
   const long long s6 = 6 * P.Nq;
+  FAME_LAUNCHED(1);
   k_vertex<R><<<grid_pts1(P.Nq, nvec, 256), 256, 0, st>>>(w0, w1, d, P.d_phase, P.nphase, ctx, P.n, s6, s6);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  FAME_LAUNCHED(1);
   k_faceedge<R><<<grid_pts1(P.Nq, nvec, 256), 256, 0, st>>>(w0, w1, d, P.d_phase, P.nphase, ctx, P.n, s6, s6);
   return cudaGetLastError();
 }
@@ -221,6 +223,7 @@ cudaError_t launch_fncB(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const
 template <class R>
 cudaError_t launch_fncA(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx, cudaStream_t st) {
   if (nvec <= 0) return cudaSuccess;
+  FAME_LAUNCHED(1);
   k_fncA<R><<<grid_pts1(P.Nq, nvec, 256), 256, 0, st>>>(x, y, pdata<R>(P), ctx, P.n);
   return cudaGetLastError();
 }
@@ -261,9 +264,11 @@ cudaError_t launch_material(const Plan& P, const cx<R>* uv, cx<R>* out, int nvec
     if (e != cudaSuccess) return e;
   }
   const PlanData<R>& d = pdata<R>(P);
+  FAME_LAUNCHED(1);
   k_phase<R, true><<<grid_pts1(P.Nq, nvec, 256), 256, 0, st>>>(out, d, ctx, P.n, 6, s6);
   e = stencil<R>(P, out, w1, nvec, ctx, st);
   if (e != cudaSuccess) return e;
+  FAME_LAUNCHED(1);
   k_phase<R, false><<<grid_pts1(P.Nq, nvec, 256), 256, 0, st>>>(out, d, ctx, P.n, 6, s6);
   return cudaGetLastError();
 }

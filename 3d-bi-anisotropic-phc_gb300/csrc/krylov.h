@@ -16,6 +16,13 @@ cudaError_t axpby_batched(const cx<R>* x, cx<R>* y, long long len, long long str
 template <class R>
 cudaError_t cg_xr(cx<R>* x, cx<R>* r, const cx<R>* p, const cx<R>* q, long long len, long long stride, int nvec,
                   const double* alpha, const int* active, cudaStream_t st);
+// out[row] = sum of partial[row][0..nblk)
+cudaError_t dot_final(const double2* partial, int nblk, int nrows, double2* out, cudaStream_t st);
+// x += alpha p ; r -= alpha q ; out[v] = (|r_v|^2, |r_v|^2) (fused)
+template <class R>
+cudaError_t cg_xr_dot(cx<R>* x, cx<R>* r, const cx<R>* p, const cx<R>* q, long long len, long long stride, int nvec,
+                      const double* alpha, const int* active, double2* out, double2* partial, int nblk,
+                      cudaStream_t st);
 template <class R>
 cudaError_t cg_p(cx<R>* p, const cx<R>* r, long long len, long long stride, int nvec, const double* beta,
                  const int* active, cudaStream_t st);
@@ -43,12 +50,13 @@ cudaError_t scale_batched(const cx<R>* x, cx<R>* y, long long len, int nvec, con
 // breakdown or a non-finite residual.
 template <class R>
 int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, double tol, int maxit,
-                int* iters_out, double* relres_out, const unsigned char* h_mask = nullptr);
+                int* iters_out, double* relres_out, const unsigned char* h_mask = nullptr,
+                const double* tol_per_vec = nullptr);
 
 // Mixed-precision B^{-1}: complex64 CG corrections inside FP64 residual
 // refinement until ||b - B x|| <= tol ||b|| (FP64).  Bx receives B*x (FP64).
 int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, const int* d_inst, double tol,
                   int max_rounds, double inner_tol32, int maxit32, const unsigned char* h_mask,
-                  long long* cg_iters, long long* b64_applies);
+                  long long* cg_iters, long long* b64_applies, const double* tol_per_vec = nullptr);
 
 }  // namespace fame

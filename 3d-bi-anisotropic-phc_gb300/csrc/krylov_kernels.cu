@@ -49,13 +49,56 @@ k_dot_partial(const cx<R>* __restrict__ a, long long a_vstride, long long a_cstr
   }
   const cx<R>* av = a + vec * a_vstride + m * a_cstride;
   const cx<R>* bv = b + vec * b_vstride;
-  double2 s = make_double2(0.0, 0.0);
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)nblk * blockDim.x) {
-    cx<R> x = av[i], y = bv[i];
-    s.x += double(x.x) * double(y.x) + double(x.y) * double(y.y);
-    s.y += double(x.x) * double(y.y) - double(x.y) * double(y.x);
+  // Per-thread partial sums in the vector's own precision (a complex64 thread
+  // sums a few dozen products; FP64 is rate-limited on this part), then FP64
+  // across threads and blocks.
+  R sx0 = 0, sy0 = 0, sx1 = 0, sy1 = 0;
+  const long long step = (long long)nblk * blockDim.x;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + step < len; i += 2 * step) {
+    cx<R> x = av[i], y = bv[i], x2 = av[i + step], y2 = bv[i + step];
+    sx0 += x.x * y.x + x.y * y.y;
+    sy0 += x.x * y.y - x.y * y.x;
+    sx1 += x2.x * y2.x + x2.y * y2.y;
+    sy1 += x2.x * y2.y - x2.y * y2.x;
   }
+  if (i < len) {
+    cx<R> x = av[i], y = bv[i];
+    sx0 += x.x * y.x + x.y * y.y;
+    sy0 += x.x * y.y - x.y * y.x;
+  }
+  double2 s = make_double2(double(sx0) + double(sx1), double(sy0) + double(sy1));
   s = block_sum2(s);
+  if (threadIdx.x == 0) *out = s;
+}
+
+// Fused CG update and residual norm: x += a p ; r -= a q ; partial |r|^2.
+template <class R>
+__global__ void __launch_bounds__(kRedThreads)
+k_cg_xr_dot(cx<R>* __restrict__ x, cx<R>* __restrict__ r, const cx<R>* __restrict__ p, const cx<R>* __restrict__ q,
+            long long len, long long stride, const double* __restrict__ alpha, const int* __restrict__ active,
+            double2* __restrict__ partial) {
+  const int vec = blockIdx.y;
+  const int nblk = gridDim.x;
+  double2* out = partial + (long long)vec * nblk + blockIdx.x;
+  if (active && !active[vec]) {
+    if (threadIdx.x == 0) *out = make_double2(0.0, 0.0);
+    return;
+  }
+  const R a = R(alpha[vec]);
+  const long long o = vec * stride;
+  R s0 = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)nblk * blockDim.x) {
+    cx<R> pi = p[o + i], qi = q[o + i], xi = x[o + i], ri = r[o + i];
+    xi.x += a * pi.x;
+    xi.y += a * pi.y;
+    ri.x -= a * qi.x;
+    ri.y -= a * qi.y;
+    x[o + i] = xi;
+    r[o + i] = ri;
+    s0 += ri.x * ri.x + ri.y * ri.y;
+  }
+  double2 s = block_sum2(make_double2(double(s0), double(s0)));
   if (threadIdx.x == 0) *out = s;
 }
 
@@ -138,16 +181,21 @@ __global__ void k_cg_scalars(int stage, int nvec, const double2* __restrict__ do
       iters[v] = -it;
     }
   } else {
-    const double rn = dot[v].x;
+    // dot = (Re r'z, |r|^2) with z = M r (z = r without preconditioner)
+    const double rz = dot[v].x;
+    const double rn = dot[v].y;
     res2[v] = rn;
-    beta[v] = rho[v] != 0.0 ? rn / rho[v] : 0.0;
-    rho[v] = rn;
+    beta[v] = rho[v] != 0.0 ? rz / rho[v] : 0.0;
+    rho[v] = rz;
     iters[v] = it;
-    if (!isfinite(rn)) {  // NaN / Inf: stop and flag
+    if (!isfinite(rn) || !isfinite(rz)) {  // NaN / Inf: stop and flag
       active[v] = 0;
       iters[v] = -it;
     } else if (rn <= tol2b2[v]) {
       active[v] = 0;  // converged: ||r|| <= tol ||b||
+    } else if (!(rz > 0.0)) {  // indefinite preconditioned system
+      active[v] = 0;
+      iters[v] = -it;
     }
   }
 }
@@ -250,7 +298,9 @@ cudaError_t dot_batched(const cx<R>* a, long long a_vstride, long long a_cstride
                         int nblk, const int* active, cudaStream_t st) {
   if (nvec <= 0 || ma <= 0) return cudaSuccess;
   dim3 g(nblk, nvec, ma);
+  FAME_LAUNCHED(1);
   k_dot_partial<R><<<g, kRedThreads, 0, st>>>(a, a_vstride, a_cstride, ma, b, b_vstride, len, partial, active);
+  FAME_LAUNCHED(1);
   k_dot_final<<<nvec * ma, kRedThreads, 0, st>>>(partial, nblk, out);
   return cudaGetLastError();
 }
@@ -261,6 +311,7 @@ cudaError_t axpby_batched(const cx<R>* x, cx<R>* y, long long len, long long str
   if (nvec <= 0) return cudaSuccess;
   int gx = grid_for(len);
   if (gx > 1024) gx = 1024;
+  FAME_LAUNCHED(1);
   k_axpby<R><<<dim3(gx, nvec), 256, 0, st>>>(x, y, len, stride, alpha, beta, active);
   return cudaGetLastError();
 }
@@ -270,7 +321,25 @@ cudaError_t cg_xr(cx<R>* x, cx<R>* r, const cx<R>* p, const cx<R>* q, long long 
                   const double* alpha, const int* active, cudaStream_t st) {
   int gx = grid_for(len);
   if (gx > 1024) gx = 1024;
+  FAME_LAUNCHED(1);
   k_cg_xr<R><<<dim3(gx, nvec), 256, 0, st>>>(x, r, p, q, len, stride, alpha, active);
+  return cudaGetLastError();
+}
+
+cudaError_t dot_final(const double2* partial, int nblk, int nrows, double2* out, cudaStream_t st) {
+  FAME_LAUNCHED(1);
+  k_dot_final<<<nrows, kRedThreads, 0, st>>>(partial, nblk, out);
+  return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t cg_xr_dot(cx<R>* x, cx<R>* r, const cx<R>* p, const cx<R>* q, long long len, long long stride, int nvec,
+                      const double* alpha, const int* active, double2* out, double2* partial, int nblk,
+                      cudaStream_t st) {
+  FAME_LAUNCHED(1);
+  k_cg_xr_dot<R><<<dim3(nblk, nvec), kRedThreads, 0, st>>>(x, r, p, q, len, stride, alpha, active, partial);
+  FAME_LAUNCHED(1);
+  k_dot_final<<<nvec, kRedThreads, 0, st>>>(partial, nblk, out);
   return cudaGetLastError();
 }
 
@@ -279,12 +348,14 @@ cudaError_t cg_p(cx<R>* p, const cx<R>* r, long long len, long long stride, int 
                  const int* active, cudaStream_t st) {
   int gx = grid_for(len);
   if (gx > 1024) gx = 1024;
+  FAME_LAUNCHED(1);
   k_cg_p<R><<<dim3(gx, nvec), 256, 0, st>>>(p, r, len, stride, beta, active);
   return cudaGetLastError();
 }
 
 cudaError_t cg_scalars(int stage, int nvec, const double2* dot, double* rho, double* alpha, double* beta,
                        const double* tol2b2, int* active, int* iters, double* res2, int it, cudaStream_t st) {
+  FAME_LAUNCHED(1);
   k_cg_scalars<<<(nvec + 127) / 128, 128, 0, st>>>(stage, nvec, dot, rho, alpha, beta, tol2b2, active, iters,
                                                     res2, it);
   return cudaGetLastError();
@@ -293,6 +364,7 @@ cudaError_t cg_scalars(int stage, int nvec, const double2* dot, double* rho, dou
 template <class R>
 cudaError_t block_rot(const cx<R>* in, cx<R>* out, long long len, long long ld, int p, int k, const double* U,
                       cudaStream_t st) {
+  FAME_LAUNCHED(1);
   k_block_rot<R><<<grid_for(len), 256, sizeof(double) * p * k, st>>>(in, out, len, ld, p, k, U);
   return cudaGetLastError();
 }
@@ -301,12 +373,14 @@ template <class R>
 cudaError_t sub_combo(cx<R>* r, const cx<R>* X, long long len, long long ld, int m, const double2* c,
                       cudaStream_t st) {
   if (m <= 0) return cudaSuccess;
+  FAME_LAUNCHED(1);
   k_sub_combo<R><<<grid_for(len), 256, sizeof(double2) * m, st>>>(r, X, len, ld, m, c);
   return cudaGetLastError();
 }
 
 template <class D, class S>
 cudaError_t convert(const cx<S>* in, cx<D>* out, long long n, cudaStream_t st) {
+  FAME_LAUNCHED(1);
   k_convert<D, S><<<grid_for(n), 256, 0, st>>>(in, out, n);
   return cudaGetLastError();
 }
@@ -314,6 +388,7 @@ cudaError_t convert(const cx<S>* in, cx<D>* out, long long n, cudaStream_t st) {
 cudaError_t refine_acc(double2* x, const float2* d, long long len, int nvec, const int* active, cudaStream_t st) {
   int gx = grid_for(len);
   if (gx > 1024) gx = 1024;
+  FAME_LAUNCHED(1);
   k_refine_acc<<<dim3(gx, nvec), 256, 0, st>>>(x, d, len, active);
   return cudaGetLastError();
 }
@@ -322,6 +397,7 @@ cudaError_t residual(const double2* b, const double2* bx, double2* res, float2* 
                      const int* active, cudaStream_t st) {
   int gx = grid_for(len);
   if (gx > 1024) gx = 1024;
+  FAME_LAUNCHED(1);
   k_residual<<<dim3(gx, nvec), 256, 0, st>>>(b, bx, res, res32, len, active);
   return cudaGetLastError();
 }
@@ -331,6 +407,7 @@ cudaError_t scale_batched(const cx<R>* x, cx<R>* y, long long len, int nvec, con
                           cudaStream_t st) {
   int gx = grid_for(len);
   if (gx > 1024) gx = 1024;
+  FAME_LAUNCHED(1);
   k_scale<R><<<dim3(gx, nvec), 256, 0, st>>>(x, y, len, s, active);
   return cudaGetLastError();
 }
@@ -348,6 +425,8 @@ template cudaError_t scale_batched<float>(const cx<float>*, cx<float>*, long lon
                                 const double*, const int*, cudaStream_t);                                 \
   template cudaError_t cg_p<R>(cx<R>*, const cx<R>*, long long, long long, int, const double*,           \
                                const int*, cudaStream_t);                                                 \
+  template cudaError_t cg_xr_dot<R>(cx<R>*, cx<R>*, const cx<R>*, const cx<R>*, long long, long long, int, \
+                                    const double*, const int*, double2*, double2*, int, cudaStream_t);    \
   template cudaError_t block_rot<R>(const cx<R>*, cx<R>*, long long, long long, int, int, const double*, \
                                     cudaStream_t);                                                        \
   template cudaError_t sub_combo<R>(cx<R>*, const cx<R>*, long long, long long, int, const double2*,     \

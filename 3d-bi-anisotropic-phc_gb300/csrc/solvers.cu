@@ -2,6 +2,9 @@
 // (fncinvB), the mixed-precision B^{-1} used by the complex64 band solve,
 // and the thick-restart Lanczos band solver of fun_Lanczos/Lanczos.m.
 #include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -14,7 +17,7 @@ namespace fame {
 
 enum WsId {
   WS_PCG_R = 0, WS_PCG_P, WS_PCG_Q, WS_PCG_SCAL, WS_PCG_PART,
-  WS_MIX_B32, WS_MIX_X32, WS_MIX_RES, WS_MIX_MASK,
+  WS_MIX_B32, WS_MIX_X32, WS_MIX_RES, WS_MIX_MASK, WS_MIX_BD, WS_PCG_Z,
   WS_LZ_Q, WS_LZ_BQ, WS_LZ_VEC, WS_LZ_TMP, WS_LZ_COEF, WS_LZ_INST, WS_LZ_MASK, WS_LZ_U, WS_LZ_SCAL, WS_LZ_DOT,
   WS_LZ_PART
 };
@@ -43,7 +46,7 @@ struct CgScalars {
 
 template <class R>
 int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, double tol, int maxit, int* iters_out,
-                double* relres_out, const unsigned char* h_mask) {
+                double* relres_out, const unsigned char* h_mask, const double* tolv) {
   if (nvec <= 0) return FAME_OK;
   cudaStream_t st = P.stream;
   const long long L = 4 * P.Nq;
@@ -77,7 +80,7 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
   std::vector<int> act(nvec, 1);
   if (h_mask)
     for (int v = 0; v < nvec; ++v) act[v] = h_mask[v] ? 1 : 0;
-  FAME_CK(cudaMemcpyAsync(S.active, act.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
+  FAME_CK(h2d_async(P, S.active, act.data(), sizeof(int) * nvec), "pcg init");
   // ||b||^2 per vector
   FAME_CK(dot_batched<R>(b, L, 0, 1, b, L, L, nvec, S.dot, part, nblk, S.active, st), "pcg dot");
   std::vector<double2> bb(nvec);
@@ -86,38 +89,62 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
   std::vector<double> rho(nvec), t2(nvec);
   for (int v = 0; v < nvec; ++v) {
     rho[v] = bb[v].x;
-    t2[v] = tol * tol * bb[v].x;
+    const double tv = tolv ? tolv[v] : tol;
+    t2[v] = tv * tv * bb[v].x;
+    if (act[v] && !std::isfinite(bb[v].x)) return fail(&P, FAME_ERR_NAN, "pcg: non-finite right-hand side");
     if (act[v] && !(bb[v].x > 0.0)) {  // zero right-hand side: x = 0
       act[v] = 0;
     }
   }
   std::vector<int> it0(nvec, 0);
-  FAME_CK(cudaMemcpyAsync(S.rho, rho.data(), sizeof(double) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
-  FAME_CK(cudaMemcpyAsync(S.tol2b2, t2.data(), sizeof(double) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
-  FAME_CK(cudaMemcpyAsync(S.res2, rho.data(), sizeof(double) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
-  FAME_CK(cudaMemcpyAsync(S.iters, it0.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
+  FAME_CK(h2d_async(P, S.rho, rho.data(), sizeof(double) * nvec), "pcg init");
+  FAME_CK(h2d_async(P, S.tol2b2, t2.data(), sizeof(double) * nvec), "pcg init");
+  FAME_CK(h2d_async(P, S.res2, rho.data(), sizeof(double) * nvec), "pcg init");
+  FAME_CK(h2d_async(P, S.iters, it0.data(), sizeof(int) * nvec), "pcg init");
   for (int v = 0; v < nvec; ++v) {
     const bool sel = h_mask ? h_mask[v] != 0 : true;
     if (!sel) continue;
     FAME_CK(cudaMemsetAsync(x + (size_t)v * L, 0, sizeof(cx<R>) * L, st), "pcg init");
   }
-  FAME_CK(cudaMemcpyAsync(S.active, act.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "pcg init");
+  FAME_CK(h2d_async(P, S.active, act.data(), sizeof(int) * nvec), "pcg init");
   FAME_CK(cudaMemcpyAsync(r, b, vb, cudaMemcpyDeviceToDevice, st), "pcg init");
-  FAME_CK(cudaMemcpyAsync(p, b, vb, cudaMemcpyDeviceToDevice, st), "pcg init");
   VecCtx ctx;
   ctx.inst = d_inst;
   ctx.active = S.active;
   ctx.nk = P.nk;
+  // Preconditioned CG (M = B0^{-1}, precond.cu) or plain CG as in fncinvB.m.
+  const bool pre = P.opt_precond != 0;
+  cx<R>* z = nullptr;
+  const int nblkv = dot_blocks(P.Nq, nvec);  // per-voxel fused kernels
+  if (pre) {
+    z = (cx<R>*)workspace(P, WS_PCG_Z + (sizeof(R) == 4 ? 100 : 0), vb, &e);
+    FAME_CK(e, "pcg workspace");
+    FAME_CK(build_precond<R>(P, st), "pcg preconditioner");
+    FAME_CK(precond_apply<R>(P, b, p, nvec, ctx, part, nblkv, st), "pcg precond");
+    FAME_CK(dot_final(part, nblkv, nvec, S.dot, st), "pcg precond");
+    std::vector<double2> rz(nvec);
+    FAME_CK(cudaMemcpyAsync(rz.data(), S.dot, sizeof(double2) * nvec, cudaMemcpyDeviceToHost, st), "pcg init");
+    FAME_CK(cudaStreamSynchronize(st), "pcg init");
+    for (int v = 0; v < nvec; ++v) rho[v] = act[v] ? rz[v].x : 0.0;
+    FAME_CK(h2d_async(P, S.rho, rho.data(), sizeof(double) * nvec), "pcg init");
+    FAME_CK(cudaStreamSynchronize(st), "pcg init");
+  } else {
+    FAME_CK(cudaMemcpyAsync(p, b, vb, cudaMemcpyDeviceToDevice, st), "pcg init");
+  }
   const int chk = 4;
   bool any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
   for (int it = 1; it <= maxit && any; ++it) {
     FAME_CK(launch_fncB<R>(P, p, q, nvec, ctx, w0, w1, st), "pcg fncB");
     FAME_CK(dot_batched<R>(p, L, 0, 1, q, L, L, nvec, S.dot, part, nblk, S.active, st), "pcg dot");
     FAME_CK(cg_scalars(0, nvec, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active, S.iters, S.res2, it, st), "pcg");
-    FAME_CK(cg_xr<R>(x, r, p, q, L, L, nvec, S.alpha, S.active, st), "pcg update");
-    FAME_CK(dot_batched<R>(r, L, 0, 1, r, L, L, nvec, S.dot, part, nblk, S.active, st), "pcg dot");
+    if (pre) {
+      FAME_CK(pcg_update<R>(P, x, r, z, p, q, nvec, ctx, S.alpha, part, nblkv, st), "pcg update");
+      FAME_CK(dot_final(part, nblkv, nvec, S.dot, st), "pcg update");
+    } else {
+      FAME_CK(cg_xr_dot<R>(x, r, p, q, L, L, nvec, S.alpha, S.active, S.dot, part, nblk, st), "pcg update");
+    }
     FAME_CK(cg_scalars(1, nvec, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active, S.iters, S.res2, it, st), "pcg");
-    FAME_CK(cg_p<R>(p, r, L, L, nvec, S.beta, S.active, st), "pcg update");
+    FAME_CK(cg_p<R>(p, pre ? z : r, L, L, nvec, S.beta, S.active, st), "pcg update");
     if (it % chk == 0 || it == maxit) {
       FAME_CK(cudaMemcpyAsync(act.data(), S.active, sizeof(int) * nvec, cudaMemcpyDeviceToHost, st), "pcg check");
       FAME_CK(cudaStreamSynchronize(st), "pcg check");
@@ -145,14 +172,15 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
 }
 
 template int pcg_batched<float>(Plan&, const float2*, float2*, int, const int*, double, int, int*, double*,
-                                const unsigned char*);
+                                const unsigned char*, const double*);
 template int pcg_batched<double>(Plan&, const double2*, double2*, int, const int*, double, int, int*, double*,
-                                 const unsigned char*);
+                                 const unsigned char*, const double*);
 
 int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, const int* d_inst, double tol,
                   int max_rounds, double inner_tol32, int maxit32, const unsigned char* h_mask, long long* cg_iters,
-                  long long* b64_applies) {
+                  long long* b64_applies, const double* tol_per_vec) {
   if (nvec <= 0) return FAME_OK;
+  auto tol_of = [&](int v) { return tol_per_vec ? tol_per_vec[v] : tol; };
   cudaStream_t st = P.stream;
   const long long L = 4 * P.Nq;
   cudaError_t e;
@@ -175,13 +203,14 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
     for (int v = 0; v < nvec; ++v) m[v] = h_mask[v] ? 1 : 0;
   std::vector<int> mi(nvec);
   for (int v = 0; v < nvec; ++v) mi[v] = m[v];
-  FAME_CK(cudaMemcpyAsync(dmask, mi.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "mixed init");
+  FAME_CK(h2d_async(P, dmask, mi.data(), sizeof(int) * nvec), "mixed init");
   FAME_CK(dot_batched<double>(b, L, 0, 1, b, L, L, nvec, dot, part, nblk, dmask, st), "mixed dot");
   std::vector<double2> bb(nvec);
   FAME_CK(cudaMemcpyAsync(bb.data(), dot, sizeof(double2) * nvec, cudaMemcpyDeviceToHost, st), "mixed init");
   FAME_CK(cudaStreamSynchronize(st), "mixed init");
   for (int v = 0; v < nvec; ++v) {
     if (!m[v]) continue;
+    if (!std::isfinite(bb[v].x)) return fail(&P, FAME_ERR_NAN, "mixed solve: non-finite right-hand side");
     FAME_CK(cudaMemsetAsync(x + (size_t)v * L, 0, sizeof(double2) * L, st), "mixed init");
     FAME_CK(cudaMemsetAsync(Bx + (size_t)v * L, 0, sizeof(double2) * L, st), "mixed init");
     if (!(bb[v].x > 0.0)) m[v] = 0;
@@ -189,25 +218,47 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
   // res = b (FP64) and its complex64 copy
   FAME_CK(residual(b, Bx, res, res32, L, nvec, dmask, st), "mixed residual");
   for (int v = 0; v < nvec; ++v) mi[v] = m[v];
-  FAME_CK(cudaMemcpyAsync(dmask, mi.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "mixed init");
+  FAME_CK(h2d_async(P, dmask, mi.data(), sizeof(int) * nvec), "mixed init");
   int rc = FAME_OK;
   std::vector<int> its(nvec);
   VecCtx ctx;
   ctx.inst = d_inst;
   ctx.active = dmask;
   ctx.nk = P.nk;
+  float2* bd32 = (float2*)workspace(P, WS_MIX_BD, sizeof(float2) * L * nvec, &e);
+  FAME_CK(e, "mixed workspace");
+  std::vector<double> rr_prev(nvec), tolv(nvec, inner_tol32);
+  for (int v = 0; v < nvec; ++v) rr_prev[v] = bb[v].x;
   for (int round = 0; round < max_rounds; ++round) {
     if (!std::any_of(m.begin(), m.end(), [](unsigned char a) { return a != 0; })) break;
-    int prc = pcg_batched<float>(P, res32, d32, nvec, d_inst, inner_tol32, maxit32, its.data(), nullptr, m.data());
+    // Complex64 CG on the current residual; after the first round only as far
+    // as the target needs (never below what complex64 resolves).
+    // (a 5x margin below the target keeps the complex64-estimated residual of
+    // the second round from missing it by a hair and costing another FP64 round)
+    for (int v = 0; v < nvec; ++v)
+      tolv[v] = round == 0 ? inner_tol32
+                           : std::min(0.5, std::max(1e-7, 0.2 * tol_of(v) * std::sqrt(bb[v].x / std::max(rr_prev[v], 1e-300))));
+    int prc = pcg_batched<float>(P, res32, d32, nvec, d_inst, inner_tol32, maxit32, its.data(), nullptr, m.data(),
+                                 tolv.data());
     if (prc == FAME_ERR_NAN || prc == FAME_ERR_BREAKDOWN) return prc;
     for (int v = 0; v < nvec; ++v)
       if (m[v] && cg_iters) *cg_iters += std::abs(its[v]);
     FAME_CK(refine_acc(x, d32, L, nvec, dmask, st), "mixed acc");
-    double2* w0 = (double2*)P.d_work;
-    double2* w1 = w0 + (size_t)nvec * 6 * P.Nq;
-    FAME_CK(launch_fncB<double>(P, x, Bx, nvec, ctx, w0, w1, st), "mixed fncB");
-    if (b64_applies)
-      for (int v = 0; v < nvec; ++v) *b64_applies += m[v];
+    if (round != 1) {
+      // exact FP64 residual b - B x
+      double2* w0 = (double2*)P.d_work;
+      double2* w1 = w0 + (size_t)nvec * 6 * P.Nq;
+      FAME_CK(launch_fncB<double>(P, x, Bx, nvec, ctx, w0, w1, st), "mixed fncB");
+      if (b64_applies)
+        for (int v = 0; v < nvec; ++v) *b64_applies += m[v];
+    } else {
+      // B x = (B x_prev) + B d with B d in complex64: d is already ~1e-6 of x,
+      // so its complex64 apply adds ~1e-13 relative error to B x.
+      float2* w0 = (float2*)P.d_work;
+      float2* w1 = w0 + (size_t)nvec * 6 * P.Nq;
+      FAME_CK(launch_fncB<float>(P, d32, bd32, nvec, ctx, w0, w1, st), "mixed fncB32");
+      FAME_CK(refine_acc(Bx, bd32, L, nvec, dmask, st), "mixed acc");
+    }
     FAME_CK(residual(b, Bx, res, res32, L, nvec, dmask, st), "mixed residual");
     FAME_CK(dot_batched<double>(res, L, 0, 1, res, L, L, nvec, dot, part, nblk, dmask, st), "mixed dot");
     std::vector<double2> rr(nvec);
@@ -216,10 +267,11 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
     for (int v = 0; v < nvec; ++v) {
       if (!m[v]) continue;
       if (!std::isfinite(rr[v].x)) return fail(&P, FAME_ERR_NAN, "mixed solve: non-finite residual");
-      if (rr[v].x <= tol * tol * bb[v].x) m[v] = 0;
+      rr_prev[v] = rr[v].x;
+      if (rr[v].x <= tol_of(v) * tol_of(v) * bb[v].x) m[v] = 0;
     }
     for (int v = 0; v < nvec; ++v) mi[v] = m[v];
-    FAME_CK(cudaMemcpyAsync(dmask, mi.data(), sizeof(int) * nvec, cudaMemcpyHostToDevice, st), "mixed mask");
+    FAME_CK(h2d_async(P, dmask, mi.data(), sizeof(int) * nvec), "mixed mask");
   }
   if (std::any_of(m.begin(), m.end(), [](unsigned char a) { return a != 0; })) rc = FAME_ERR_NOT_CONVERGED;
   return rc;
@@ -239,6 +291,7 @@ struct LzInst {
   double beta = 0.0;
   std::vector<double> U;  // final Ritz combination, p x k0 column-major
   long long steps = 0, restarts = 0, bapplies = 0, cgits = 0;
+  double itol = 1e-12;  // inner B^{-1} tolerance of this instance (mixed form: scaled by the spectral spread)
 };
 
 int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double tol, int maxit, int p,
@@ -284,16 +337,17 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
   double2* part = (double2*)workspace(P, WS_LZ_PART, sizeof(double2) * std::max(nblk1 * 64, nblkb * na) + 64, &e);
   FAME_CK(e, "lanczos workspace");
   FAME_CK(ensure_work(P, na), "lanczos scratch");
-  FAME_CK(cudaMemcpyAsync(dinst, insts.data(), sizeof(int) * na, cudaMemcpyHostToDevice, st), "lanczos init");
+  FAME_CK(h2d_async(P, dinst, insts.data(), sizeof(int) * na), "lanczos init");
 
   std::vector<LzInst> S(na);
   for (int a = 0; a < na; ++a) {
     S[a].inst = insts[a];
     S[a].k0 = S[a].k = k0;
+    S[a].itol = itol;
   }
   std::vector<int> mask(na, 1);
   auto upload_mask = [&]() -> cudaError_t {
-    return cudaMemcpyAsync(dmask, mask.data(), sizeof(int) * na, cudaMemcpyHostToDevice, st);
+    return h2d_async(P, dmask, mask.data(), sizeof(int) * na);
   };
   FAME_CK(upload_mask(), "lanczos init");
   VecCtx ctx;
@@ -312,7 +366,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     return FAME_OK;
   };
   auto scale_vecs = [&](const double2* x, double2* y, const std::vector<double>& s) -> int {
-    FAME_CK(cudaMemcpyAsync(dsc, s.data(), sizeof(double) * na, cudaMemcpyHostToDevice, st), "lanczos scale");
+    FAME_CK(h2d_async(P, dsc, s.data(), sizeof(double) * na), "lanczos scale");
     FAME_CK(scale_batched<double>(x, y, L, na, dsc, dmask, st), "lanczos scale");
     return FAME_OK;
   };
@@ -331,11 +385,9 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     double2* Qa = Q + (size_t)a * p * L;
     double2* BQa = BQ + (size_t)a * p * L;
     double2* ca = coef + (size_t)a * 128 + 64;
-    FAME_CK(cudaMemcpyAsync(ca, cs.data(), sizeof(double2) * cs.size(), cudaMemcpyHostToDevice, st), "lanczos");
+    FAME_CK(h2d_async(P, ca, cs.data(), sizeof(double2) * cs.size()), "lanczos");
     FAME_CK(sub_combo<double>(r, Qa + (size_t)col0 * L, L, L, (int)cs.size(), ca, st), "lanczos");
     if (br) FAME_CK(sub_combo<double>(br, BQa + (size_t)col0 * L, L, L, (int)cs.size(), ca, st), "lanczos");
-    // keep cs alive until the copy has been consumed
-    FAME_CK(cudaStreamSynchronize(st), "lanczos");
     return FAME_OK;
   };
   const bool mixed = prec == FAME_C64;
@@ -346,7 +398,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     std::vector<double2> hv(L);
     for (long long i = 0; i < L; ++i) hv[i] = v0_host ? make_double2(v0_host[2 * i], v0_host[2 * i + 1]) : make_double2(1.0, 0.0);
     for (int a = 0; a < na; ++a)
-      FAME_CK(cudaMemcpyAsync(V + (size_t)a * L, hv.data(), cb, cudaMemcpyHostToDevice, st), "lanczos v0");
+      FAME_CK(h2d_async(P, V + (size_t)a * L, hv.data(), cb), "lanczos v0");
     FAME_CK(fncB64(V, BV), "lanczos v0");
     total_b += na;
     std::vector<double2> vb;
@@ -360,6 +412,29 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
   const double eps = 2.2204e-16;  // Lanczos.m:23
   int rc_final = FAME_OK;
   std::vector<unsigned char> hm(na);
+  // FAME_PROFILE=1 prints the wall time of each phase of the Lanczos step
+  // (the stream is synchronised at every phase boundary while it is on).
+  struct PhaseTimer {
+    bool on = false;
+    cudaStream_t st = nullptr;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    std::chrono::steady_clock::time_point t0;
+    void start() {
+      if (!on) return;
+      cudaStreamSynchronize(st);
+      t0 = std::chrono::steady_clock::now();
+    }
+    void mark(int i) {
+      if (!on) return;
+      cudaStreamSynchronize(st);
+      auto t1 = std::chrono::steady_clock::now();
+      acc[i] += std::chrono::duration<double>(t1 - t0).count();
+      t0 = t1;
+    }
+  } prof;
+  prof.on = std::getenv("FAME_PROFILE") != nullptr;
+  prof.st = st;
+  prof.start();
   while (true) {
     bool any = false;
     for (int a = 0; a < na; ++a) {
@@ -380,11 +455,14 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     std::vector<double2> al;
     int rc = batched_dot(AQ, V, al);
     if (rc) return rc;
+    prof.mark(0);
     // pr = fncBinv(r)   (Lanczos.m:54,57,61)
     for (int a = 0; a < na; ++a) hm[a] = mask[a];
     if (mixed) {
       long long cgi = 0, b64 = 0;
-      rc = solve_B_mixed(P, AQ, PR, BPR, na, dinst, itol, 6, 1e-6, 2000, hm.data(), &cgi, &b64);
+      std::vector<double> tv(na);
+      for (int a = 0; a < na; ++a) tv[a] = S[a].itol;
+      rc = solve_B_mixed(P, AQ, PR, BPR, na, dinst, itol, 8, P.opt_tol32, 2000, hm.data(), &cgi, &b64, tv.data());
       if (rc == FAME_ERR_NAN || rc == FAME_ERR_BREAKDOWN) return rc;
       total_b += b64;
       for (int a = 0; a < na; ++a)
@@ -399,6 +477,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
           total_b += std::abs(its[a]);
         }
     }
+    prof.mark(1);
     // orthogonalisation (Lanczos.m:53-69)
     for (int a = 0; a < na; ++a) {
       if (S[a].done) continue;
@@ -422,6 +501,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
       if ((rc = project_out(a, r, br, 0, I.j))) return rc;
       I.steps++;
     }
+    prof.mark(2);
     // rr = fncB(r); beta = sqrt(r'*rr); v = r/beta  (Lanczos.m:72-74)
     if (!mixed) {
       FAME_CK(fncB64(PR, BPR), "lanczos fncB");
@@ -441,6 +521,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     }
     if ((rc = scale_vecs(PR, V, s))) return rc;
     if ((rc = scale_vecs(BPR, BV, s))) return rc;
+    prof.mark(3);
     // cycle ends
     for (int a = 0; a < na; ++a) {
       if (S[a].done) continue;
@@ -487,6 +568,15 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         I.done = true;
         continue;
       }
+      if (mixed) {
+        // The error an inexact B^{-1} leaves in a Ritz pair is amplified by
+        // lambda_max / lambda_j in its residual (near Gamma the shifted
+        // zero modes have lambda ~ 1e4); tighten this instance's inner
+        // tolerance by the spread of the wanted Ritz values.
+        const double lmax = std::fabs(w[ind[0]]), lk = std::fabs(w[ind[I.k0 - 1]]);
+        const double spread = lmax > 0.0 ? std::min(1.0, lk / lmax) : 1.0;
+        I.itol = std::max(1e-15, itol * spread);
+      }
       int k = I.k0 + std::min(nconv, (p - I.k0) / 2);  // :122
       if (k == 1 && p > 3) k = p / 2;
       std::vector<double> Uk((size_t)np * k);
@@ -498,7 +588,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         I.c[c2] = I.beta * Uk[(size_t)c2 * np + np - 1];  // :140
       }
       // Q(:,1:k) = Q*U ; BQ likewise (Lanczos.m:135-137)
-      FAME_CK(cudaMemcpyAsync(dU, Uk.data(), sizeof(double) * Uk.size(), cudaMemcpyHostToDevice, st), "lz restart");
+      FAME_CK(h2d_async(P, dU, Uk.data(), sizeof(double) * Uk.size()), "lz restart");
       double2* Qa = Q + (size_t)a * p * L;
       double2* BQa = BQ + (size_t)a * p * L;
       FAME_CK(block_rot<double>(Qa, TMP, L, L, np, k, dU, st), "lz restart");
@@ -513,7 +603,12 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
       I.mm++;
       I.restarts++;
     }
+    prof.mark(4);
   }
+  if (prof.on)
+    std::fprintf(stderr,
+                 "[fame lanczos] instances %d: fncA+alpha %.3fs  B^-1 %.3fs  reorth %.3fs  beta %.3fs  restart %.3fs\n",
+                 na, prof.acc[0], prof.acc[1], prof.acc[2], prof.acc[3], prof.acc[4]);
   // Ritz vectors ev = Q*U(:, ind(1:k0)) (Lanczos.m:146-152) and outputs
   double2* EV = ev;
   for (int a = 0; a < na; ++a) {
@@ -533,7 +628,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     for (int a = 0; a < na; ++a) {
       LzInst& I = S[a];
       const int np = (int)(I.U.size() / k0);
-      FAME_CK(cudaMemcpyAsync(dU, I.U.data(), sizeof(double) * I.U.size(), cudaMemcpyHostToDevice, st), "lz ritz");
+      FAME_CK(h2d_async(P, dU, I.U.data(), sizeof(double) * I.U.size()), "lz ritz");
       FAME_CK(block_rot<double>(Q + (size_t)a * p * L, TMP, L, L, np, k0, dU, st), "lz ritz");
       if (EV) FAME_CK(cudaMemcpyAsync(EV + (size_t)a * k0 * L, TMP, cb * k0, cudaMemcpyDeviceToDevice, st), "lz ritz");
       if (res) {
@@ -543,7 +638,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         std::vector<int> ii(k0, I.inst);
         int* di = (int*)workspace(P, WS_LZ_INST + 50, sizeof(int) * k0, &e);
         FAME_CK(e, "lz res");
-        FAME_CK(cudaMemcpyAsync(di, ii.data(), sizeof(int) * k0, cudaMemcpyHostToDevice, st), "lz res");
+        FAME_CK(h2d_async(P, di, ii.data(), sizeof(int) * k0), "lz res");
         c1.inst = di;
         double2* AX = (double2*)workspace(P, WS_LZ_INST + 51, cb * k0, &e);
         FAME_CK(e, "lz res");
@@ -559,25 +654,25 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
           cl[i] = make_double2(I.d[i], 0.0);
           cb0[i] = make_double2(-1.0, 0.0);
         }
-        // AX <- AX - lambda BX
+        // NFSEP residual of EvaluteError_Chiral_no_inv.m:20 for the
+        // B-normalised Ritz vector x: || B x - omega A x ||, omega = 1/lambda.
+        // AX <- BX - omega AX
         double2* al2 = (double2*)workspace(P, WS_LZ_INST + 53, sizeof(double2) * 2 * k0, &e);
         FAME_CK(e, "lz res");
-        std::vector<double2> ms(k0);
-        for (int i = 0; i < k0; ++i) ms[i] = make_double2(-I.d[i], 0.0);
-        std::vector<double2> ones(k0, make_double2(1.0, 0.0));
-        FAME_CK(cudaMemcpyAsync(al2, ms.data(), sizeof(double2) * k0, cudaMemcpyHostToDevice, st), "lz res");
-        FAME_CK(cudaMemcpyAsync(al2 + k0, ones.data(), sizeof(double2) * k0, cudaMemcpyHostToDevice, st), "lz res");
+        std::vector<double2> ones(k0, make_double2(1.0, 0.0)), mw(k0);
+        for (int i = 0; i < k0; ++i) mw[i] = make_double2(-1.0 / I.d[i], 0.0);
+        FAME_CK(h2d_async(P, al2, ones.data(), sizeof(double2) * k0), "lz res");
+        FAME_CK(h2d_async(P, al2 + k0, mw.data(), sizeof(double2) * k0), "lz res");
         FAME_CK(axpby_batched<double>(BX, AX, L, L, k0, al2, al2 + k0, nullptr, st), "lz res");
         const int nb = dot_blocks(L, k0);
         double2* pp = (double2*)workspace(P, WS_LZ_INST + 54, sizeof(double2) * (nb * k0 + 2 * k0) + 64, &e);
         FAME_CK(e, "lz res");
         double2* o1 = pp + (size_t)nb * k0;
         FAME_CK(dot_batched<double>(AX, L, 0, 1, AX, L, L, k0, o1, pp, nb, nullptr, st), "lz res");
-        FAME_CK(dot_batched<double>(TMP, L, 0, 1, TMP, L, L, k0, o1 + k0, pp, nb, nullptr, st), "lz res");
-        std::vector<double2> h2(2 * k0);
-        FAME_CK(cudaMemcpyAsync(h2.data(), o1, sizeof(double2) * 2 * k0, cudaMemcpyDeviceToHost, st), "lz res");
+        std::vector<double2> h2(k0);
+        FAME_CK(cudaMemcpyAsync(h2.data(), o1, sizeof(double2) * k0, cudaMemcpyDeviceToHost, st), "lz res");
         FAME_CK(cudaStreamSynchronize(st), "lz res");
-        for (int i = 0; i < k0; ++i) res[(size_t)a * k0 + i] = std::sqrt(h2[i].x / h2[k0 + i].x);
+        for (int i = 0; i < k0; ++i) res[(size_t)a * k0 + i] = std::sqrt(std::max(0.0, h2[i].x));
       }
     }
     FAME_CK(cudaStreamSynchronize(st), "lz out");

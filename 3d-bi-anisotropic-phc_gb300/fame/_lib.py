@@ -25,6 +25,8 @@ FAME_C128 = 0
 FAME_C64 = 1
 FAME_PR, FAME_QR, FAME_PRS, FAME_QRS = 0, 1, 2, 3
 FAME_HOST_PTR = 1
+FAME_OPT_PRECOND = 0
+FAME_OPT_TOL32 = 1
 
 STATUS_NAMES = {0: "OK", 1: "BAD_ARG", 2: "CUDA", 3: "NOT_CONVERGED", 4: "BREAKDOWN", 5: "NAN",
                 6: "UNSUPPORTED", 7: "SINGULAR", 8: "ALLOC"}
@@ -40,9 +42,11 @@ _pll = C.POINTER(C.c_longlong)
 
 SIGNATURES = {
     "fame_version": (C.c_char_p, []),
+    "fame_kernel_launches": (C.c_longlong, []),
     "fame_plan_create": (_i, [C.POINTER(_vp), _i, _i, _pd, C.POINTER(C.c_uint8), _i, _pd]),
     "fame_plan_destroy": (_i, [_vp]),
     "fame_set_stream": (_i, [_vp, _vp]),
+    "fame_set_option": (_i, [_vp, _i, _d]),
     "fame_sync": (_i, [_vp]),
     "fame_last_error": (C.c_char_p, [_vp]),
     "fame_plan_info": (_i, [_vp, _pi, _pi, _pll]),

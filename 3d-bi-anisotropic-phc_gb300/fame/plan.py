@@ -103,6 +103,12 @@ class Plan:
     def sync(self):
         check(self._lib.fame_sync(self._h), self._h, "fame_sync")
 
+    def set_option(self, option, value):
+        """fame_set_option: 'precond' (bool) or 'tol32' (float)."""
+        code = {"precond": L.FAME_OPT_PRECOND, "tol32": L.FAME_OPT_TOL32}.get(option, option)
+        check(self._lib.fame_set_option(self._h, int(code), float(value)), self._h, "fame_set_option")
+        return self
+
     # -- generic call -------------------------------------------------------
     def _call(self, fn, x, out_len, inst, *extra, name=""):
         prec = _prec_of(x)

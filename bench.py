@@ -1,0 +1,381 @@
+#!/usr/bin/env python3
+"""Headline benchmark: k-point band solves per second on one GB300.
+
+Workload: the woodpile photonic crystal of the reference's band-structure
+script at n = 60 (FCC, a = 1, rods of width 0.25a, eps = 13, mu = 1,
+xi = -zeta = 0.2i inside, vacuum outside), the 40-point band path
+Gamma-X-U|K-Gamma-L-W-X, 10 bands per k-point, Lanczos tolerance 1e-10 as in
+the reference, every eigenpair checked with FP64 matvecs to the reference's
+NFSEP residual ||B x - omega A x|| <= 1e-8 for the B-normalised eigenvector x
+(fun_no_inv/EvaluteError_Chiral_no_inv.m:20).  A step solves one batch of `--batch` k-points of the path
+in one batched band solve (complex64 matvecs and inner CG, FP64 Lanczos
+recurrence, reorthogonalisation, residual refinement and Ritz check); five
+steps of 8 cover the whole path.
+
+Prints one JSON line (rank 0).  `--impl reference` times the reference's
+algorithm on the host cores instead (the FP64 CPU restatement; MATLAB is not
+available on this machine).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKGDIR = os.path.join(ROOT, "3d-bi-anisotropic-phc_gb300")
+for _p in (PKGDIR, ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "k-point band solves/s at n=60, res<=1e-8 (batched mixed complex64/FP64, woodpile, 10 bands)"
+UNIT = "k-point solves/s"
+N_GRID = 60
+BANDS = 10
+LANCZOS_TOL = 1e-10
+INNER_TOL = 1e-12          # B^{-1} of the plain FP64 form (the reference's pcg tolerance)
+INNER_TOL_MIXED = 1e-12    # B^{-1} of the mixed form (complex64 CG + FP64 residual refinement;
+                           # tightened per k-point by the Ritz-value spread, see solvers.cu)
+RES_TOL = 1e-8
+PATH_POINTS = 40
+# B applies (fncB) of one plain-FP64 Lanczos band solve at n = 60 on this path
+# (mean over k-points of the FP64 GPU form's stats); used to extrapolate the
+# CPU timings, which can only afford a bounded sample of fncB applications.
+FP64_B_APPLIES_PER_KPOINT = 12000
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per complex64 fncB at n=60 from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "fncb_c64_n60_ncu.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_fncB_vector:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join("/tmp", f"fame_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.remove(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def path_batches(batch):
+    import fame
+
+    path = fame.band_path(npts=PATH_POINTS)
+    nb = max(1, PATH_POINTS // batch)
+    return path, [path[i * batch:(i + 1) * batch] for i in range(nb)]
+
+
+def run_fame(args):
+    import torch
+    import torch.distributed as dist
+
+    import fame
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = fame.load()
+    path, batches = path_batches(args.batch)
+    nb = len(batches)
+    bidx = lambda s: (s * world + rank) % nb
+    needed = sorted({bidx(s) for s in range(args.warmup + args.steps)})
+    plans = {b: fame.woodpile_plan(N_GRID, batches[b]) for b in needed}
+
+    def solve(plan):
+        return plan.band_solve(BANDS, tol=LANCZOS_TOL, prec="c64", inner_tol=INNER_TOL_MIXED)
+
+    for s in range(args.warmup):
+        solve(plans[bidx(s)])
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.fame_kernel_launches()
+    clocks.start()
+    e0.record(stream)
+    results = []
+    for s in range(args.steps):
+        results.append(solve(plans[bidx(args.warmup + s)]))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = lib.fame_kernel_launches() - launches0
+    if world > 1:
+        dist.barrier()
+    t = e0.elapsed_time(e1) / 1000.0
+    tmax = t
+    if world > 1:
+        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tmax = float(tt.item())
+    nk_total = args.steps * args.batch * world
+    value = nk_total / tmax
+    res_max = max(float(np.max(r["res"])) for r in results)
+    status = [int(r["status"]) for r in results]
+    steps = np.concatenate([r["stats"][:, 0] for r in results])
+    cgits = np.concatenate([r["stats"][:, 3] for r in results])
+
+    # ---- end to end through the C ABI with host buffers -------------------
+    import fame.handles as H
+
+    e2e_steps = max(0, min(args.steps, args.e2e_steps))
+    A = fame.fcc_lattice()
+    inside = fame.woodpile_inside(fame.vertex_positions(N_GRID, A), 0.25)
+    phase_host = torch.from_numpy(inside.astype(np.uint8)).pin_memory().numpy()
+    tens = np.stack([fame.covariant_blocks(fame.bi_isotropic(1.0, 0.0), A),
+                     fame.covariant_blocks(fame.bi_isotropic(13.0, 0.2), A)])
+    h2d = d2h = 0
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        kv = batches[bidx(s)]
+        th = np.stack([fame.bloch_angles(k, A) for k in kv])
+        with fame.Plan(N_GRID, th, phase_host, tens) as pl:
+            r = pl.band_solve(BANDS, tol=LANCZOS_TOL, prec="c64", inner_tol=INNER_TOL_MIXED)
+        h2d += phase_host.nbytes + th.nbytes + tens.nbytes * len(kv)
+        d2h += r["ew"].nbytes + r["res"].nbytes + r["stats"].nbytes
+    torch.cuda.synchronize()
+    te = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([te], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        te = float(tt.item())
+    e2e_value = e2e_steps * args.batch * world / te if e2e_steps else None
+
+    out = None
+    if rank == 0:
+        # ---- roofline of the dominant operator: complex64 fncB ------------
+        plan = plans[needed[0]]
+        L = 4 * N_GRID ** 3
+        x = torch.randn(args.batch, L, dtype=torch.complex64, device="cuda")
+        for _ in range(3):
+            plan.apply_B(x)
+        torch.cuda.synchronize()
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 20
+        r0.record(stream)
+        for _ in range(reps):
+            plan.apply_B(x)
+        r1.record(stream)
+        torch.cuda.synchronize()
+        t_b = r0.elapsed_time(r1) / 1000.0 / reps
+        Nq = N_GRID ** 3
+        alg_bytes = args.batch * (32 * Nq * 8 + Nq)
+        peak, peak_kind = measured_peak_hbm()
+        achieved = alg_bytes / t_b / 1e9
+        traffic = profile_traffic()
+        roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                    "traffic": None if traffic is None else round(traffic * args.batch),
+                    "kernel": f"fncB complex64 n=60, {args.batch} vectors per launch sequence",
+                    "launch_us": round(t_b * 1e6, 1)}
+        # ---- plain FP64 form on a sample of the same path ---------------------
+        fp64 = None
+        if args.fp64_kpoints > 0:
+            fb = 1 if nb > 1 else 0  # a batch without the Gamma point, whose shifted zero modes
+            kv = batches[fb][:args.fp64_kpoints]  # double the count of B applies
+            p64 = fame.woodpile_plan(N_GRID, kv)
+            p64.set_option("precond", 0)  # the reference's unpreconditioned pcg (fncinvB.m)
+            torch.cuda.synchronize()
+            f0 = time.perf_counter()
+            r64 = p64.band_solve(BANDS, tol=LANCZOS_TOL, prec="c128", inner_tol=INNER_TOL)
+            torch.cuda.synchronize()
+            t64 = time.perf_counter() - f0
+            ew_mixed = None
+            for s, r in enumerate(results):
+                if bidx(args.warmup + s) == fb:
+                    ew_mixed = r["ew"][:args.fp64_kpoints]
+            if ew_mixed is None:
+                pm = fame.woodpile_plan(N_GRID, kv)
+                ew_mixed = pm.band_solve(BANDS, tol=LANCZOS_TOL, prec="c64", inner_tol=INNER_TOL_MIXED)["ew"]
+                pm.close()
+            err = float(np.max(np.abs(ew_mixed - r64["ew"]) / np.abs(r64["ew"])))
+            v64 = args.fp64_kpoints / t64
+            fp64 = {"value": round(v64, 5), "unit": UNIT, "kpoints": args.fp64_kpoints,
+                    "b_applies_per_kpoint": float(np.mean(r64["stats"][:, 2])),
+                    "max_res": float(np.max(r64["res"])), "speedup_mixed_vs_fp64": round(value / v64, 2),
+                    "max_rel_eig_err_mixed_vs_fp64": err}
+            p64.close()
+        # ---- CPU baseline: the FP64 restatement on the host cores --------------
+        cpu = None
+        if world == 1 and args.cpu_seconds > 0:
+            nb_fp64 = fp64["b_applies_per_kpoint"] if fp64 else FP64_B_APPLIES_PER_KPOINT
+            cpu = cpu_baseline(args.cpu_seconds, nb_fp64)
+        out = {
+            "metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(tmax / args.steps * 1e3, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64/f64", "data": "synthetic (woodpile geometry, "
+            "band path generated in-run)",
+            "config": {"workload": "woodpile n=60 (FCC a=1, rod width 0.25a, eps=13, xi=-zeta=0.2i), "
+                                   "40-point path G-X-U|K-G-L-W-X, 10 bands, Lanczos tol 1e-10, res<=1e-8",
+                       "n": N_GRID, "bands": BANDS, "kpoints_per_step": args.batch, "path_kpoints": PATH_POINTS,
+                       "precision": "complex64 fncB + preconditioned CG, FP64 recurrence/reorth/residual "
+                                    "refinement (B^-1 to 1e-11)/Ritz check",
+                       "l2": "inputs larger than L2 (Lanczos basis and B*Q of a batch ~4.4 GB)"},
+            "e2e": {"value": None if e2e_value is None else round(e2e_value, 5), "unit": UNIT,
+                    "h2d_bytes_per_step": int(h2d / max(1, e2e_steps)),
+                    "d2h_bytes_per_step": int(d2h / max(1, e2e_steps)), "steps": e2e_steps,
+                    "path": "fame_plan_create (host geometry/material) + fame_band_solve + results to host"},
+            "roofline": roofline, "gpu_launches": int(launches), "clocks": clk,
+            "max_residual": res_max, "res_ok": bool(res_max <= RES_TOL), "status": status,
+            "lanczos_steps_mean": float(np.mean(steps)), "cg_iters_per_kpoint_mean": float(np.mean(cgits)),
+            "fp64": fp64, "cpu_baseline": cpu,
+        }
+    for p in plans.values():
+        p.close()
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+def _oracle_problem():
+    import oracle as O
+
+    O.fft_workers(os.cpu_count() or 1)
+    return O.build_problem(N_GRID, wave_vec=O.fcc_vertex("X"), gamma=0.2)
+
+
+def cpu_baseline(seconds, b_applies):
+    """Time the oracle's fncB (scipy.sparse + pocketfft, FP64) at n=60 for about
+    `seconds` and extrapolate one k-point solve as `b_applies` applications."""
+    P = _oracle_problem()
+    x = np.ones(4 * N_GRID ** 3, dtype=np.complex128)
+    P.B(x)
+    t0 = time.perf_counter()
+    cnt = 0
+    while time.perf_counter() - t0 < seconds:
+        P.B(x)
+        cnt += 1
+    tb = (time.perf_counter() - t0) / cnt
+    return {"value": round(1.0 / (tb * b_applies), 8), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{cnt} FP64 oracle fncB applications at n=60 (X point), {tb * 1e3:.1f} ms each; one "
+                      f"k-point solve extrapolated as {b_applies:.0f} applications (FP64 Lanczos + CG count)"}
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    P = _oracle_problem()
+    x = np.ones(4 * N_GRID ** 3, dtype=np.complex128)
+    for _ in range(args.warmup):
+        P.B(x)
+    per = max(1, args.ref_applies)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for _ in range(per):
+            P.B(x)
+        times.append((time.perf_counter() - t0) / per)
+    tb = statistics.median(times)
+    v = 1.0 / (tb * FP64_B_APPLIES_PER_KPOINT)
+    sample = (f"{per} FP64 oracle fncB applications per step at n=60 (X point), {tb * 1e3:.1f} ms each; "
+              f"one k-point solve = {FP64_B_APPLIES_PER_KPOINT} applications (FP64 Lanczos + CG count)")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(tb * per * 1e3, 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": "woodpile n=60, 10 bands, Lanczos tol 1e-10 (CPU restatement of the MATLAB "
+                               "path; MATLAB unavailable on this box)", "n": N_GRID, "bands": BANDS},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=8, help="k-points per step (batched band solve)")
+    ap.add_argument("--impl", choices=["fame", "reference"], default="fame")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--fp64-kpoints", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-applies", type=int, default=10)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_fame(args)
+
+
+if __name__ == "__main__":
+    main()

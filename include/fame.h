@@ -50,6 +50,10 @@ enum fame_handle { FAME_PR = 0, FAME_QR = 1, FAME_PRS = 2, FAME_QRS = 3 };
 /* Library version string. */
 const char* fame_version(void);
 
+/* Kernels launched by this library since it was loaded (all plans); a
+ * diagnostic for benchmarks, no reference counterpart. */
+long long fame_kernel_launches(void);
+
 /*
  * Create a plan for `nk` k-points of one n^3 grid.
  *   theta   [nk*3]   Bloch angles theta_d = k . a_d per instance
@@ -69,6 +73,15 @@ int fame_plan_create(fame_plan_t* plan, int n, int nk, const double* theta, cons
 int fame_plan_destroy(fame_plan_t plan);
 /* Use `stream` (a cudaStream_t) for all later calls on this plan. */
 int fame_set_stream(fame_plan_t plan, void* stream);
+
+/* Solver options (no reference counterpart; defaults in brackets):
+ *   FAME_OPT_PRECOND  CG on B preconditioned by the averaged-medium block
+ *                     inverse B0^{-1} [1]; 0 gives the reference's
+ *                     unpreconditioned pcg of fncinvB.m.
+ *   FAME_OPT_TOL32    complex64 CG tolerance of the first refinement round of
+ *                     the mixed-precision B^{-1} [1e-6]. */
+enum fame_option { FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1 };
+int fame_set_option(fame_plan_t plan, int option, double value);
 int fame_sync(fame_plan_t plan);
 const char* fame_last_error(fame_plan_t plan);
 int fame_plan_info(fame_plan_t plan, int* n, int* nk, long long* nq);
@@ -115,7 +128,8 @@ int fame_apply_material(fame_plan_t plan, int prec, const void* x, void* y, int 
  *                   reorthogonalisation and a final FP64 refinement.
  * Outputs: ew[k] eigenvalues of B^{-1}A, descending (omega = 1/ew);
  * ev (device, complex128, 4Nq x k, may be NULL) B-normalised Ritz vectors;
- * res[k] (may be NULL) ||B x - omega A x|| / ||B x|| with FP64 matvecs;
+ * res[k] (may be NULL) the NFSEP residual ||B x - omega A x|| of the
+ * B-normalised Ritz vector with FP64 matvecs (EvaluteError_Chiral_no_inv.m:20);
  * stats[4] (may be NULL): Lanczos steps, restarts, B applies, inner CG iterations.
  * Replaces fun_Lanczos/Lanczos.m:1-167 (with op_invB of
  * band_structure_woodpile_Lanczos_n60_gamma0p2.m:74-81).

@@ -10,14 +10,17 @@ import oracle as O
 
 def random_tensors(rng, nphase, hermitian=True):
     """Per-phase covariant N, M, J blocks (27 complex).  Hermitian N, M
-    diagonal-dominant blocks mimic physical materials; hermitian=False gives
-    general complex blocks (exercises the (X+X')/2 symmetrisation)."""
+    diagonal-dominant blocks with a weak J mimic physical materials (B is then
+    positive definite, as CG needs); hermitian=False gives general complex
+    blocks (exercises the (X+X')/2 symmetrisation)."""
     out = np.zeros((nphase, 27), dtype=np.complex128)
     for p in range(nphase):
         for b in range(3):
             m = rng.standard_normal((3, 3)) + 1j * rng.standard_normal((3, 3))
             if hermitian and b < 2:
                 m = 0.5 * (m + m.conj().T) * 0.2 + np.eye(3) * (1.0 + p)
+            elif hermitian:
+                m = 0.1 * m  # weak coupling keeps [M J'; J N] positive definite
             out[p, b * 9:(b + 1) * 9] = m.ravel()
     return out
 

@@ -118,6 +118,29 @@ def test_fncinvB_c64(cuda, fame_lib):
     assert relerr(back, x) < 3e-5
 
 
+def test_fncinvB_reports_breakdown_and_nan(cuda, fame_lib):
+    # Failure detection on the host: an indefinite B (strong J coupling) makes CG
+    # break down (p'Bp <= 0) and a NaN right-hand side yields FAME_ERR_NAN; both
+    # come back as status codes, the context stays usable.
+    n = 6
+    I3 = np.eye(3).ravel()
+    tens = np.concatenate([I3, I3, 3.0 * I3]).astype(complex)[None, :]
+    plan = fame.Plan(n, [[0.4, -0.2, 1.1]], np.zeros(n ** 3, np.uint8), tens)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(4 * n ** 3) + 1j * rng.standard_normal(4 * n ** 3)
+    with pytest.raises(fame.FameError) as e:
+        plan.apply_Binv(_dev(x, "c128"), tol=1e-10, maxit=500, raise_on_noconv=True)
+    assert e.value.code == 4
+    P = Pair(6, nk=1, seed=3)
+    xn = P.vec(4 * P.Nq)
+    xn[5] = np.nan
+    with pytest.raises(fame.FameError) as e:
+        P.plan.apply_Binv(_dev(xn, "c128"), tol=1e-10, maxit=50, raise_on_noconv=True)
+    assert e.value.code in (4, 5)
+    y = P.plan.apply_B(_dev(P.vec(4 * P.Nq), "c128"))  # still usable
+    assert np.isfinite(y.cpu().numpy()).all()
+
+
 def test_errors(cuda, fame_lib):
     import torch
 
