@@ -177,7 +177,9 @@ template <class R> void free_tables(PlanData<R>& d) {
 int check_singular(Plan& P) {
   const int n = P.n;
   const double w[3] = {1.0 / std::sqrt(14.0), 2.0 / std::sqrt(14.0), 3.0 / std::sqrt(14.0)};
+  P.sigma_min.assign(P.nk, 0.0);
   for (int k = 0; k < P.nk; ++k) {
+    double lqmin = 1e300;
     std::vector<std::complex<double>> l(3 * n);
     for (int ax = 0; ax < 3; ++ax)
       for (int j = 0; j < n; ++j) {
@@ -189,6 +191,7 @@ int check_singular(Plan& P) {
         for (int i1 = 0; i1 < n; ++i1) {
           std::complex<double> L[3] = {l[i1], l[n + i2], l[2 * n + i3]};
           double lq = std::norm(L[0]) + std::norm(L[1]) + std::norm(L[2]);
+          lqmin = std::min(lqmin, lq);
           std::complex<double> lw = w[0] * L[0] + w[1] * L[1] + w[2] * L[2];
           double n1 = lq - std::norm(lw);
           if (!(lq > 0.0) || !(n1 > 1e-300)) {
@@ -200,6 +203,7 @@ int check_singular(Plan& P) {
             return fail(&P, FAME_ERR_SINGULAR, buf);
           }
         }
+    P.sigma_min[k] = std::sqrt(lqmin);
   }
   return FAME_OK;
 }

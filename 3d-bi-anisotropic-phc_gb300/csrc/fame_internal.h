@@ -46,6 +46,7 @@ struct Plan {
   int opt_precond = 1;                // CG on B preconditioned by the averaged-medium B0^{-1}
   double opt_tol32 = 1e-6;            // complex64 CG tolerance of the first refinement round
   std::vector<double> theta;          // [nk][3]
+  std::vector<double> sigma_min;      // [nk] smallest curl singular value sqrt(min |L|^2)
   std::vector<double> mat_avg;        // [nk][27][2] volume-averaged Herm(N) | Herm(M) | J
   double2* d_mat_avg = nullptr;       // device copy
   std::vector<double> mat_host;       // [nk][nphase][27][2] covariant N | M | J blocks

@@ -292,6 +292,8 @@ struct LzInst {
   std::vector<double> U;  // final Ritz combination, p x k0 column-major
   long long steps = 0, restarts = 0, bapplies = 0, cgits = 0;
   double itol = 1e-12;  // inner B^{-1} tolerance of this instance (mixed form: scaled by the spectral spread)
+  bool explicit_br = false;  // mixed form: B r by an FP64 apply instead of the recurrence
+  bool refresh_bq = false;   // recompute the kept B*Q columns in FP64 at this restart
 };
 
 int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double tol, int maxit, int p,
@@ -344,6 +346,14 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     S[a].inst = insts[a];
     S[a].k0 = S[a].k = k0;
     S[a].itol = itol;
+    if (prec == FAME_C64 && P.sigma_min[insts[a]] < 1e-2) {
+      // A near-zero wave vector (Gamma shifted by 1e-4) gives curl singular
+      // values ~1e-4 and eigenvalues lambda ~ 1e4 among the wanted ones: run
+      // this instance with the tightest inner solves and explicit FP64 B r
+      // from the first step (see the spread rule at the restarts).
+      S[a].itol = 1e-15;
+      S[a].explicit_br = true;
+    }
   }
   std::vector<int> mask(na, 1);
   auto upload_mask = [&]() -> cudaError_t {
@@ -506,6 +516,23 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     if (!mixed) {
       FAME_CK(fncB64(PR, BPR), "lanczos fncB");
       for (int a = 0; a < na; ++a) total_b += mask[a];
+    } else {
+      // Instances with an extreme Ritz-value spread (the shifted zero modes
+      // near Gamma) take B r by an explicit FP64 apply, as Lanczos.m:72 does:
+      // a 1e-13 error in the cached B*q columns would leave a component of
+      // the lambda ~ 1e4 modes that the other bands' residuals amplify.
+      bool anyx = false;
+      std::vector<int> xm(na, 0);
+      for (int a = 0; a < na; ++a) {
+        xm[a] = (!S[a].done && S[a].explicit_br) ? 1 : 0;
+        anyx |= xm[a] != 0;
+      }
+      if (anyx) {
+        FAME_CK(h2d_async(P, dmask, xm.data(), sizeof(int) * na), "lanczos mask");
+        FAME_CK(fncB64(PR, BPR), "lanczos fncB");
+        FAME_CK(upload_mask(), "lanczos mask");
+        for (int a = 0; a < na; ++a) total_b += xm[a];
+      }
     }
     std::vector<double2> rr;
     if ((rc = batched_dot(PR, BPR, rr))) return rc;
@@ -576,6 +603,8 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         const double lmax = std::fabs(w[ind[0]]), lk = std::fabs(w[ind[I.k0 - 1]]);
         const double spread = lmax > 0.0 ? std::min(1.0, lk / lmax) : 1.0;
         I.itol = std::max(1e-15, itol * spread);
+        I.refresh_bq = !I.explicit_br && spread < 1e-3;
+        I.explicit_br = spread < 1e-3;
       }
       int k = I.k0 + std::min(nconv, (p - I.k0) / 2);  // :122
       if (k == 1 && p > 3) k = p / 2;
@@ -595,6 +624,21 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
       FAME_CK(cudaMemcpyAsync(Qa, TMP, cb * k, cudaMemcpyDeviceToDevice, st), "lz restart");
       FAME_CK(block_rot<double>(BQa, TMP, L, L, np, k, dU, st), "lz restart");
       FAME_CK(cudaMemcpyAsync(BQa, TMP, cb * k, cudaMemcpyDeviceToDevice, st), "lz restart");
+      if (I.refresh_bq) {
+        // first restart of a Gamma-like instance: exact FP64 B*Q for the kept columns
+        std::vector<int> ii(k, I.inst);
+        int* di = (int*)workspace(P, WS_LZ_INST + 60, sizeof(int) * k, &e);
+        FAME_CK(e, "lz restart");
+        FAME_CK(h2d_async(P, di, ii.data(), sizeof(int) * k), "lz restart");
+        FAME_CK(ensure_work(P, std::max(k, na)), "lz restart");
+        VecCtx ck;
+        ck.inst = di;
+        ck.nk = P.nk;
+        double2* w0 = (double2*)P.d_work;
+        FAME_CK(launch_fncB<double>(P, Qa, BQa, k, ck, w0, w0 + (size_t)k * 6 * P.Nq, st), "lz restart");
+        total_b += k;
+        I.refresh_bq = false;
+      }
       FAME_CK(cudaStreamSynchronize(st), "lz restart");
       I.k = k;
       I.justRestarted = true;
