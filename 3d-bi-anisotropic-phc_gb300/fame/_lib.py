@@ -52,6 +52,7 @@ SIGNATURES = {
     "fame_plan_info": (_i, [_vp, _pi, _pi, _pll]),
     "fame_apply_A": (_i, [_vp, _i, _vp, _vp, _i, _pi, _i]),
     "fame_apply_B": (_i, [_vp, _i, _vp, _vp, _i, _pi, _i]),
+    "fame_apply_B_noalloc": (_i, [_vp, _i, _vp, _vp, _i]),
     "fame_apply_Binv": (_i, [_vp, _i, _vp, _vp, _i, _pi, _d, _i, _pi, _pd, _i]),
     "fame_curl_transform": (_i, [_vp, _i, _i, _vp, _vp, _i, _pi, _i]),
     "fame_apply_handle": (_i, [_vp, _i, _i, _vp, _vp, _i, _pi, _i]),

@@ -93,7 +93,8 @@ class Plan:
         self.close()
 
     @property
-    def handle(self):
+    def raw(self):
+        """The fame_plan_t handle (ctypes c_void_p) for direct C-ABI calls."""
         return self._h
 
     def _stream(self):

@@ -93,6 +93,18 @@ int fame_apply_A(fame_plan_t plan, int prec, const void* x, void* y, int nvec, c
  * fun_no_inv/fncB_Generate_no_inv.m:1-9. */
 int fame_apply_B(fame_plan_t plan, int prec, const void* x, void* y, int nvec, const int* inst, int flags);
 
+/* y = B x like fame_apply_B, for callers that cannot let a library allocate
+ * device memory at call time (a MEX gateway under MATLAB's gpuArray memory
+ * manager, an application pooling its whole device budget).  It allocates
+ * nothing: its scratch is one fixed 16 MiB device array of the library,
+ * whose address is looked up on the first call on each device (make that call
+ * before any stream capture).  x and y are device pointers, vector v belongs
+ * to instance v % nk; requests needing more than 16 MiB of scratch
+ * (nvec * 12 * n^3 * element size) are rejected with FAME_ERR_BAD_ARG.  All
+ * calls share the array: calls whose kernels overlap on the GPU race.
+ * No counterpart in the reference. */
+int fame_apply_B_noalloc(fame_plan_t plan, int prec, const void* x, void* y, int nvec);
+
 /* y = B^{-1} x by conjugate gradients to relative residual `tol` within
  * `maxit` iterations per vector; iters/relres (may be NULL) receive per-vector
  * results.  Returns FAME_ERR_NOT_CONVERGED if any vector missed `tol`.
