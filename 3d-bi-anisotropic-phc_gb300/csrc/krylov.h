@@ -31,6 +31,19 @@ cudaError_t cg_scalars(int stage, int nvec, const double2* dot, double* rho, dou
 template <class R>
 cudaError_t block_rot(const cx<R>* in, cx<R>* out, long long len, long long ld, int p, int k, const double* U,
                       cudaStream_t st);
+// out = a x + b y + c w with real scalars (y, w may be null; out may alias x)
+template <class R>
+cudaError_t lincomb3(cx<R>* out, double a, const cx<R>* x, double b, const cx<R>* y, double c, const cx<R>* w,
+                     long long len, cudaStream_t st);
+// MINRES on the Hermitian (indefinite) operator B - shift A for one vector
+// of instance `inst` (d_inst: device int[1]); tol relative to ||b||.
+template <class R>
+int minres_shifted(Plan& P, const cx<R>* b, cx<R>* x, const int* d_inst, double shift, double tol, int maxit,
+                   int* iters, double* relres);
+// out[:, j] = sum_i in[:, i] * C[i, j], C complex m x q column-major (<= 12800 entries)
+template <class R>
+cudaError_t block_comb(const cx<R>* in, cx<R>* out, long long len, long long ld, int m, int q, const double2* C,
+                       cudaStream_t st);
 template <class R>
 cudaError_t sub_combo(cx<R>* r, const cx<R>* X, long long len, long long ld, int m, const double2* c,
                       cudaStream_t st);

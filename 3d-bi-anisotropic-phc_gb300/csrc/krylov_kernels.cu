@@ -220,6 +220,48 @@ __global__ void k_block_rot(const cx<R>* __restrict__ in, cx<R>* __restrict__ ou
   }
 }
 
+// out = a x + b y + c w (real scalars; y, w may be null)
+template <class R>
+__global__ void k_lincomb3(cx<R>* out, double a, const cx<R>* x, double b, const cx<R>* y, double c, const cx<R>* w,
+                           long long len) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    cx<R> xi = x[i];
+    double rx = a * xi.x, ry = a * xi.y;
+    if (y) {
+      cx<R> yi = y[i];
+      rx += b * yi.x;
+      ry += b * yi.y;
+    }
+    if (w) {
+      cx<R> wi = w[i];
+      rx += c * wi.x;
+      ry += c * wi.y;
+    }
+    out[i] = mk<R>(R(rx), R(ry));
+  }
+}
+
+// out[:, j] = sum_i in[:, i] * C[i, j]  (C complex m x q, column-major)
+template <class R>
+__global__ void k_block_comb(const cx<R>* __restrict__ in, cx<R>* __restrict__ out, long long len, long long ld,
+                             int m, int q, const double2* __restrict__ C) {
+  extern __shared__ double2 Cs[];
+  for (int i = threadIdx.x; i < m * q; i += blockDim.x) Cs[i] = C[i];
+  __syncthreads();
+  for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < len; row += (long long)gridDim.x * blockDim.x) {
+    for (int j = 0; j < q; ++j) {
+      double sx = 0.0, sy = 0.0;
+      for (int i = 0; i < m; ++i) {
+        const cx<R> v = in[(long long)i * ld + row];
+        const double2 c = Cs[j * m + i];
+        sx += double(v.x) * c.x - double(v.y) * c.y;
+        sy += double(v.x) * c.y + double(v.y) * c.x;
+      }
+      out[(long long)j * ld + row] = mk<R>(R(sx), R(sy));
+    }
+  }
+}
+
 // r -= sum_i c_i X[:, i]  (complex coefficients, FP64)
 template <class R>
 __global__ void k_sub_combo(cx<R>* __restrict__ r, const cx<R>* __restrict__ X, long long len, long long ld, int m,
@@ -368,6 +410,34 @@ cudaError_t block_rot(const cx<R>* in, cx<R>* out, long long len, long long ld, 
   k_block_rot<R><<<grid_for(len), 256, sizeof(double) * p * k, st>>>(in, out, len, ld, p, k, U);
   return cudaGetLastError();
 }
+
+template <class R>
+cudaError_t lincomb3(cx<R>* out, double a, const cx<R>* x, double b, const cx<R>* y, double c, const cx<R>* w,
+                     long long len, cudaStream_t st) {
+  FAME_LAUNCHED(1);
+  k_lincomb3<R><<<grid_for(len), 256, 0, st>>>(out, a, x, b, y, c, w, len);
+  return cudaGetLastError();
+}
+template cudaError_t lincomb3<float>(cx<float>*, double, const cx<float>*, double, const cx<float>*, double,
+                                     const cx<float>*, long long, cudaStream_t);
+template cudaError_t lincomb3<double>(cx<double>*, double, const cx<double>*, double, const cx<double>*, double,
+                                      const cx<double>*, long long, cudaStream_t);
+
+template <class R>
+cudaError_t block_comb(const cx<R>* in, cx<R>* out, long long len, long long ld, int m, int q, const double2* C,
+                       cudaStream_t st) {
+  const size_t sm = sizeof(double2) * m * q;
+  if (sm > 200 * 1024) return cudaErrorInvalidValue;
+  if (sm > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_block_comb<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+  }
+  FAME_LAUNCHED(1);
+  k_block_comb<R><<<grid_for(len), 256, sm, st>>>(in, out, len, ld, m, q, C);
+  return cudaGetLastError();
+}
+template cudaError_t block_comb<double>(const cx<double>*, cx<double>*, long long, long long, int, int, const double2*,
+                                        cudaStream_t);
 
 template <class R>
 cudaError_t sub_combo(cx<R>* r, const cx<R>* X, long long len, long long ld, int m, const double2* c,

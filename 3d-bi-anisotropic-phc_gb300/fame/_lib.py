@@ -60,6 +60,7 @@ SIGNATURES = {
     "fame_lanczos": (_i, [_vp, _i, _i, _i, _d, _i, _i, _pd, _d, _pd, _vp, _pd, _pll]),
     "fame_band_solve": (_i, [_vp, _i, _i, _d, _i, _i, _d, _pd, _pd, _pll]),
     "fame_material_blocks": (_i, [_pd, _pd, _pd]),
+    "fame_jdsira": (_i, [_vp, _i, _i, _i, _d, _d, _d, _i, _i, _d, _i, _pd, _vp, _pd, _pll]),
 }
 
 

@@ -216,6 +216,30 @@ class Plan:
             check(rc, self._h, "fame_lanczos")
         return dict(ew=ew, omega=1.0 / ew, res=res, ev=ev, stats=stats, status=rc)
 
+    def jdsira(self, nev, target=0.0, tol=1e-8, no_restart=50, restart_dim=4, inner_tol=1e-2, inner_maxit=30000,
+               inst=0, inner_prec="c64", want_vectors=False, shift=0.0):
+        """SIRA with locking (GEP_AB_Herm_JDSIRA_Driver4.m called as Driver4(fncB, fncA, ...)):
+        the `nev` eigenvalues of fncB x = theta fncA x closest to `target`.
+        Returns dict(ew, res, ev, stats, status)."""
+        ew = np.zeros(nev, dtype=np.float64)
+        res = np.zeros(nev, dtype=np.float64)
+        stats = np.zeros(4, dtype=np.int64)
+        pd = C.POINTER(C.c_double)
+        ev = None
+        evp = None
+        if want_vectors:
+            ev = torch.empty((nev, 4 * self.Nq), dtype=torch.complex128, device="cuda")
+            evp = C.c_void_p(ev.data_ptr())
+        self._stream()
+        pr = L.FAME_C64 if inner_prec in ("c64", L.FAME_C64) else L.FAME_C128
+        rc = self._lib.fame_jdsira(self._h, pr, int(inst), int(nev), float(target), float(shift), float(tol),
+                                   int(no_restart),
+                                   int(restart_dim), float(inner_tol), int(inner_maxit), ew.ctypes.data_as(pd), evp,
+                                   res.ctypes.data_as(pd), stats.ctypes.data_as(C.POINTER(C.c_longlong)))
+        if rc not in (L.FAME_OK, L.FAME_ERR_NOT_CONVERGED):
+            check(rc, self._h, "fame_jdsira")
+        return dict(ew=ew, res=res, ev=ev, stats=stats, status=rc)
+
     def band_solve(self, k, tol=1e-10, maxit=10000, p=None, prec="c64", inner_tol=1e-12):
         """All instances at once (fame_band_solve).  Returns dict(ew, omega, res, stats, status)."""
         p = 2 * k if p is None else p

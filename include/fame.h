@@ -158,6 +158,26 @@ int fame_band_solve(fame_plan_t plan, int prec, int k, double tol, int maxit, in
                     double* ew, double* res, long long* stats);
 
 /*
+ * Interior eigenpairs by SIRA with locking: the `nev` eigenvalues theta of
+ * fncB x = theta fncA x (theta = omega) closest to `target`, residual
+ * ||B u - theta A u|| <= tol for unit u.  Search space of at most
+ * `no_restart` + locked vectors, restarts keep `restart_dim` Ritz vectors;
+ * SIRA corrections t = (B - shift A)^{-1} r in `inner_prec` (FAME_C64 or
+ * FAME_C128) to relative tolerance `inner_tol` within `inner_maxit`
+ * iterations: shift = 0 is the reference's correction (its shift term is
+ * commented out) solved by CG, shift != 0 the shifted correction by MINRES.
+ * Outputs: ew[nev] (NaN where not converged), ev (device complex128
+ * 4Nq x nev, may be NULL) unit eigenvectors, res[nev] (may be NULL),
+ * stats[4] (may be NULL): outer steps, inner CG iterations, B applies,
+ * pairs converged.  Replaces light_locked_Huang/GEP_AB_Herm_JDSIRA_Driver4.m:1-82
+ * with GEP_AB_Herm_JDSIRA_Locking4.m and SIRA_solve_residual_LS_GEP.m
+ * (called as Driver4(fncB, fncA, ...) in main_EIG_np_*.m).
+ */
+int fame_jdsira(fame_plan_t plan, int inner_prec, int inst, int nev, double target, double shift, double tol,
+                int no_restart, int restart_dim, double inner_tol, int inner_maxit, double* ew, void* ev, double* res,
+                long long* stats);
+
+/*
  * Covariant material blocks of one phase: invert the 6x6 constitutive block
  * [eps xi; zeta mu] (row-major, interleaved complex, 36*2 doubles), split it
  * and return A'*X*A of the (1,1), (2,2) and (1,2) blocks as 27 complex
