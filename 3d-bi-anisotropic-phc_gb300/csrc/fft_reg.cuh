@@ -1,7 +1,14 @@
 // In-register mixed-radix FFT of compile-time length N (N = 2^a 3^b 5^c).
 //
-// One thread owns one pencil of N complex values in registers.  The
-// transform is Cooley-Tukey with the first radix split off (N = R*M):
+// One thread owns one pencil of N complex values in registers.  A length
+// with coprime factors N = N1*N2 (N1 the full power of its smallest prime)
+// is split by the prime-factor (Good-Thomas) mapping, which needs no twiddle
+// factors:
+//   n = (N2*n1 + N1*n2) mod N,   k = (N2*A*k1 + N1*B*k2) mod N,
+//   A = N2^{-1} mod N1, B = N1^{-1} mod N2,
+//   X[k] = sum_{n2} W_N2^{n2*k2} sum_{n1} x[n] W_N1^{n1*k1}.
+// A prime power is split by Cooley-Tukey with the first radix split off
+// (N = R*M):
 //   X[k1 + R*k2] = sum_{n2} W_N^{n2*k1} W_M^{n2*k2} sum_{n1} x[M*n1 + n2] W_R^{n1*k1}
 // i.e. M radix-R butterflies on strided inputs, a twiddle, then R
 // recursive length-M transforms.  All indices are compile-time constants,
@@ -17,6 +24,26 @@ namespace fame {
 
 FAME_HD constexpr int fft_first_radix(int n) {
   return (n % 4 == 0 && n != 8) ? 4 : (n % 2 == 0) ? 2 : (n % 3 == 0) ? 3 : (n % 5 == 0) ? 5 : n;
+}
+
+// Full power of the smallest prime factor of n (n itself for a prime power).
+FAME_HD constexpr int fft_pfa_part(int n) {
+  int p = 2;
+  while (p < n && n % p != 0) ++p;
+  int q = 1;
+  while (n % p == 0) {
+    n /= p;
+    q *= p;
+  }
+  return q;
+}
+
+// a^{-1} mod m for coprime a, m (m >= 1).
+FAME_HD constexpr int fft_inv_mod(int a, int m) {
+  if (m == 1) return 0;
+  for (int x = 1; x < m; ++x)
+    if ((a * x) % m == 1) return x;
+  return -1;
 }
 
 FAME_HD constexpr bool fft_supported(int n) {
@@ -103,7 +130,34 @@ FAME_HD void dft_small(cx<R> (&a)[P]) {
 template <class R, int N, int S>
 FAME_HD void fft(cx<R> (&x)[N]) {
   constexpr int RD = fft_first_radix(N);
+  constexpr int N1 = fft_pfa_part(N);
   if constexpr (N == 1) {
+  } else if constexpr (N1 > 1 && N1 < N) {
+    constexpr int N2 = N / N1;
+    constexpr int A = fft_inv_mod(N2 % N1, N1);
+    constexpr int B = fft_inv_mod(N1 % N2, N2);
+    static_assert(A >= 0 && B >= 0, "prime-factor split needs coprime factors");
+    cx<R> y[N];  // y[k1*N2 + n2]
+    static_for<0, N2>([&](auto n2c) {
+      constexpr int n2 = decltype(n2c)::value;
+      cx<R> a[N1];
+      static_for<0, N1>([&](auto n1c) {
+        constexpr int n1 = decltype(n1c)::value;
+        a[n1] = x[(N2 * n1 + N1 * n2) % N];
+      });
+      fft<R, N1, S>(a);
+      static_for<0, N1>([&](auto k1c) { y[decltype(k1c)::value * N2 + n2] = a[decltype(k1c)::value]; });
+    });
+    static_for<0, N1>([&](auto k1c) {
+      constexpr int k1 = decltype(k1c)::value;
+      cx<R> z[N2];
+      static_for<0, N2>([&](auto n2c) { z[decltype(n2c)::value] = y[k1 * N2 + decltype(n2c)::value]; });
+      fft<R, N2, S>(z);
+      static_for<0, N2>([&](auto k2c) {
+        constexpr int k2 = decltype(k2c)::value;
+        x[(N2 * A * k1 + N1 * B * k2) % N] = z[k2];
+      });
+    });
   } else if constexpr (RD == N) {
     dft_small<R, N, S>(x);
   } else {

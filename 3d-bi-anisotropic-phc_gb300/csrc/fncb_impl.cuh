@@ -23,10 +23,10 @@
 // where Mh, Nh are the Hermitian parts of the vertex tensors: (X + X^H)/2 of
 // the assembled operator equals the operator built from Herm(A).
 //
-// Pipeline (this file, one launch each):
+// Pipeline (one launch each):
 //   plane_inv  : Pi blocks per frequency voxel + inverse DFT along x and y
 //   col        : inverse DFT along z (in place)
-//   vertex     : U, V, Hu, Hv at every vertex
+//   vertex     : U, V, Hu, Hv at every vertex (fncb_material.cuh)
 //   faceedge   : u', v' (in place over u, v)
 //   col        : forward DFT along z
 //   plane_fwd  : forward DFT along y and x + Pi^H blocks
@@ -38,6 +38,7 @@
 
 #include "fame_internal.h"
 #include "fft_reg.cuh"
+#include "fncb_material.cuh"
 
 namespace fame {
 namespace detail {
@@ -59,9 +60,9 @@ __device__ __forceinline__ PiBlock<R> pi_block(cx<R> lx, cx<R> ly, cx<R> lz) {
   R lq = lx.x * lx.x + lx.y * lx.y + ly.x * ly.x + ly.y * ly.y + lz.x * lz.x + lz.y * lz.y;
   cx<R> lw = mk<R>(w1 * lx.x + w2 * ly.x + w3 * lz.x, w1 * lx.y + w2 * ly.y + w3 * lz.y);
   R n1sq = lq - (lw.x * lw.x + lw.y * lw.y);
-  R inv1 = R(1) / sqrt(n1sq);
-  R sq = sqrt(lq);
-  R inv0 = R(1) / sq;
+  R inv1 = rsqrt(n1sq);
+  R inv0 = rsqrt(lq);
+  R sq = lq * inv0;
   cx<R> b0 = cconj(lx), b1 = cconj(ly), b2 = cconj(lz);
   PiBlock<R> P;
   P.p1[0] = cscale(csub(cscale(b1, w3), cscale(b2, w2)), inv1);
@@ -89,7 +90,7 @@ template <class R> __device__ __forceinline__ R rsqrt_n3(int n) {
 // S_x S_y when WITH_S.
 // ---------------------------------------------------------------------------
 template <class R, int N, bool PREP, bool WITH_S>
-__global__ void __launch_bounds__(((3 * N + 31) / 32) * 32)
+__global__ void __launch_bounds__(((3 * N + 31) / 32) * 32, sizeof(R) == 4 ? 2 : 1)
 k_plane_inv(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d, VecCtx ctx,
             long long in_stride, long long in_side_stride, long long out_stride, int side0) {
   constexpr int LD = N + 1;
@@ -105,30 +106,54 @@ k_plane_inv(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d,
   const cx<R>* xin = x + vec * in_stride + blockIdx.y * in_side_stride + (long long)k3 * N * N;
   const int tid = threadIdx.x;
 
-  for (int e = tid; e < N * N; e += blockDim.x) {
-    const int i2 = e / N, i1 = e - i2 * N;
-    cx<R> v0, v1, v2;
-    if constexpr (PREP) {
-      PiBlock<R> P = pi_block<R>(lam[i1], lam[N + i2], lam[2 * N + k3]);
-      cx<R> a = xin[e], b = xin[Nq + e];
-      if (side == 0) {
-        v0 = cfmac(P.p1[0], b, cneg(cmulc(P.p2[0], a)));
-        v1 = cfmac(P.p1[1], b, cneg(cmulc(P.p2[1], a)));
-        v2 = cfmac(P.p1[2], b, cneg(cmulc(P.p2[2], a)));
-      } else {
-        v0 = cfma(P.p2[0], b, cmul(P.p1[0], a));
-        v1 = cfma(P.p2[1], b, cmul(P.p1[1], a));
-        v2 = cfma(P.p2[2], b, cmul(P.p1[2], a));
+  // Input plane -> shared memory.  The global loads of PF elements per thread
+  // are issued together before any is used, so a CTA waits for one memory
+  // round trip per batch instead of one per element.
+  constexpr int T = ((3 * N + 31) / 32) * 32;
+  constexpr int ITEMS = (N * N + T - 1) / T;
+  constexpr int NB = PREP ? 2 : 3;                        // input blocks
+  constexpr int PF0 = (sizeof(R) == 4 ? 24 : 12) / NB;   // elements in flight per thread
+  constexpr int PF = PF0 < ITEMS ? PF0 : ITEMS;
+  static_for<0, (ITEMS + PF - 1) / PF>([&](auto bc) {
+    constexpr int base = decltype(bc)::value * PF;
+    cx<R> in[PF][NB];
+#pragma unroll
+    for (int it = 0; it < PF; ++it) {
+      const int e = tid + (base + it) * T;
+      if (base + it < ITEMS && e < N * N) {
+#pragma unroll
+        for (int c = 0; c < NB; ++c) in[it][c] = xin[c * Nq + e];
       }
-    } else {
-      v0 = xin[e];
-      v1 = xin[Nq + e];
-      v2 = xin[2 * Nq + e];
     }
-    sm[(0 * N + i2) * LD + i1] = v0;
-    sm[(1 * N + i2) * LD + i1] = v1;
-    sm[(2 * N + i2) * LD + i1] = v2;
-  }
+#pragma unroll
+    for (int it = 0; it < PF; ++it) {
+      const int e = tid + (base + it) * T;
+      if (base + it < ITEMS && e < N * N) {
+        const int i2 = e / N, i1 = e - i2 * N;
+        cx<R> v0, v1, v2;
+        if constexpr (PREP) {
+          PiBlock<R> P = pi_block<R>(lam[i1], lam[N + i2], lam[2 * N + k3]);
+          const cx<R> a = in[it][0], b = in[it][1];
+          if (side == 0) {
+            v0 = cfmac(P.p1[0], b, cneg(cmulc(P.p2[0], a)));
+            v1 = cfmac(P.p1[1], b, cneg(cmulc(P.p2[1], a)));
+            v2 = cfmac(P.p1[2], b, cneg(cmulc(P.p2[2], a)));
+          } else {
+            v0 = cfma(P.p2[0], b, cmul(P.p1[0], a));
+            v1 = cfma(P.p2[1], b, cmul(P.p1[1], a));
+            v2 = cfma(P.p2[2], b, cmul(P.p1[2], a));
+          }
+        } else {
+          v0 = in[it][0];
+          v1 = in[it][1];
+          v2 = in[it][NB - 1];
+        }
+        sm[(0 * N + i2) * LD + i1] = v0;
+        sm[(1 * N + i2) * LD + i1] = v1;
+        sm[(2 * N + i2) * LD + i1] = v2;
+      }
+    }
+  });
   __syncthreads();
   if (tid < 3 * N) {  // x rows
     const int c = tid / N, i2 = tid - c * N;
@@ -171,7 +196,7 @@ k_plane_inv(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d,
 // else copies the 3 components out.
 // ---------------------------------------------------------------------------
 template <class R, int N, bool POST, bool WITH_S>
-__global__ void __launch_bounds__(((3 * N + 31) / 32) * 32)
+__global__ void __launch_bounds__(((3 * N + 31) / 32) * 32, sizeof(R) == 4 ? 2 : 1)
 k_plane_fwd(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, VecCtx ctx,
             long long w_stride, long long out_stride, long long out_side_stride, int side0) {
   constexpr int LD = N + 1;
@@ -215,7 +240,9 @@ k_plane_fwd(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, V
   __syncthreads();
   const cx<R>* lam = d.lam + (long long)inst * 3 * N;
   cx<R>* o = y + vec * out_stride + blockIdx.y * out_side_stride + (long long)k3 * N * N;
-  for (int e = tid; e < N * N; e += blockDim.x) {
+  constexpr int T = ((3 * N + 31) / 32) * 32;
+#pragma unroll 4
+  for (int e = tid; e < N * N; e += T) {
     const int i2 = e / N, i1 = e - i2 * N;
     cx<R> u0 = sm[(0 * N + i2) * LD + i1];
     cx<R> u1 = sm[(1 * N + i2) * LD + i1];
@@ -246,7 +273,7 @@ k_plane_fwd(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, V
 // (forward).  Scale 1/sqrt(n).
 // ---------------------------------------------------------------------------
 template <class R, int N, int DIR, int SMODE>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 3 : 1)
 k_col(cx<R>* __restrict__ w, PlanData<R> d, VecCtx ctx, long long stride) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   const int f = blockIdx.y;
@@ -315,13 +342,6 @@ cudaError_t col(const PlanData<R>& d, cx<R>* w, int nfield, int nvec, long long 
   return cudaGetLastError();
 }
 
-template <class R> inline const PlanData<R>& pdata(const Plan& P);
-template <> inline const PlanData<double>& pdata<double>(const Plan& P) { return P.d64; }
-template <> inline const PlanData<float>& pdata<float>(const Plan& P) { return P.d32; }
-
-// Material stencil (fncb_stencil.cu): periodic-frame [M J^H; J N] in place on w0, scratch w1.
-template <class R>
-cudaError_t stencil(const Plan& P, cx<R>* w0, cx<R>* w1, int nvec, const VecCtx& ctx, cudaStream_t st);
 
 template <class R, int N>
 cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx, cx<R>* w0, cx<R>* w1,
@@ -333,7 +353,7 @@ cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecC
   if (e != cudaSuccess) return e;
   e = col<R, N, +1, 0>(d, w0, 6, nvec, 6 * Nq, ctx, st);
   if (e != cudaSuccess) return e;
-  e = stencil<R>(P, w0, w1, nvec, ctx, st);
+  e = stencil_n<R, N>(P, w0, w1, nvec, ctx, st);
   if (e != cudaSuccess) return e;
   e = col<R, N, -1, 0>(d, w0, 6, nvec, 6 * Nq, ctx, st);
   if (e != cudaSuccess) return e;
@@ -384,12 +404,16 @@ cudaError_t handle_n(const Plan& P, int which, const cx<R>* x, cx<R>* y, int nve
 }  // namespace detail
 }  // namespace fame
 
-#define FAME_SIZE_SIGS(R, NN)                                                                                      \
-  cudaError_t fame::detail::fncB_n<R, NN>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&, cx<R>*, cx<R>*,   \
-                                          cudaStream_t);                                                           \
-  template cudaError_t fame::detail::transform_n<R, NN>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&, \
-                                                        cudaStream_t);                                             \
-  template cudaError_t fame::detail::handle_n<R, NN>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&,    \
-                                                     cx<R>*, cudaStream_t);
+// Declarations of the size-templated entry points of one (precision, size),
+// each prefixed by PFX ("template" to instantiate, "extern template" to
+// suppress instantiation in other translation units).
+#define FAME_SIZE_SIGS(PFX, R, NN)                                                                                 \
+  PFX cudaError_t fame::detail::fncB_n<R, NN>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&, cx<R>*,       \
+                                              cx<R>*, cudaStream_t);                                               \
+  PFX cudaError_t fame::detail::stencil_n<R, NN>(const Plan&, cx<R>*, cx<R>*, int, const VecCtx&, cudaStream_t);  \
+  PFX cudaError_t fame::detail::transform_n<R, NN>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&,     \
+                                                   cudaStream_t);                                                  \
+  PFX cudaError_t fame::detail::handle_n<R, NN>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&,        \
+                                                cx<R>*, cudaStream_t);
 // explicit instantiation of one (precision, size)
-#define FAME_INST_SIZE(R, NN) template FAME_SIZE_SIGS(R, NN)
+#define FAME_INST_SIZE(R, NN) FAME_SIZE_SIGS(template, R, NN)
