@@ -169,6 +169,7 @@ template <class R> void free_tables(PlanData<R>& d) {
   cudaFree(d.sxyz);
   cudaFree(d.mat);
   cudaFree(d.pc);
+  cudaFree(d.fld);
   d = PlanData<R>();
 }
 
@@ -314,6 +315,7 @@ int fame_plan_destroy(fame_plan_t h) {
   cudaFree(P.d_red);
   cudaFree(P.d_stage);
   cudaFree(P.d_mat_avg);
+  cudaFree(P.d_eps_gam);
   if (P.h_ring) cudaFreeHost(P.h_ring);
   free_workspaces(P);
   delete h;

@@ -33,6 +33,12 @@ template <class R> struct PlanData {
   cx<R>* sxyz = nullptr; // [nk][3n]  S_sDFT per axis (the MtxVecMul_FFT phase)
   cx<R>* mat = nullptr;  // [nk][nphase][27]: Herm(N) | Herm(M) | J, row-major 3x3 each
   cx<R>* pc = nullptr;   // [nk][10][Nq] CG preconditioner: inverse 4x4 Hermitian blocks (lazy)
+  // Field mode (per-vertex isotropic chiral medium eps(r) I, mu = I,
+  // xi = -zeta = i gamma(r) I): vertex tensors N = a G, M = b G, J = -i g G with
+  // a = 1/(eps - gamma^2), b = eps a, g = gamma a and G = A^T A the lattice
+  // Gram matrix.  fld = [3][Nq] a | b | g, or null in phase-table mode.
+  R* fld = nullptr;
+  R gram[9] = {};
 };
 
 struct Plan {
@@ -51,6 +57,10 @@ struct Plan {
   double2* d_mat_avg = nullptr;       // device copy
   std::vector<double> mat_host;       // [nk][nphase][27][2] covariant N | M | J blocks
   uint8_t* d_phase = nullptr;         // [Nq] phase id per vertex
+  bool field_mode = false;            // per-vertex (eps, gamma) instead of phase ids
+  double lattice[9] = {};             // field mode: primitive vectors as columns (row-major)
+  std::vector<double> eps_host, gam_host;  // field mode: [Nq] each
+  double* d_eps_gam = nullptr;        // field mode: [2][Nq] eps | gamma (FP64, gradient)
   PlanData<double> d64;
   PlanData<float> d32;
   // scratch: two 6-field work buffers per vector, sized for complex128
@@ -91,6 +101,11 @@ cudaError_t launch_fncB(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const
 template <class R>
 cudaError_t launch_fncA(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,
                         cudaStream_t st);
+// First half of fncB: w = [u; v] = periodic-frame inverse DFT of [Pi.Pr x1; Pi.Qr x2]
+// (6-field vectors, stride 6*Nq).
+template <class R>
+cudaError_t launch_fields_inv(const Plan& P, const cx<R>* x, cx<R>* w, int nvec, const VecCtx& ctx,
+                              cudaStream_t st);
 // MtxVecMul_FFT on 3Nq vectors: trans = 0 'notranspose' (S .* ifftn*sqrt(N)),
 // 1 'transpose' (fftn(conj(S).*x)/sqrt(N)).
 template <class R>

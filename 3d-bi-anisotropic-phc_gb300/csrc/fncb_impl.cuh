@@ -361,6 +361,15 @@ cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecC
 }
 
 template <class R, int N>
+cudaError_t fields_inv_n(const Plan& P, const cx<R>* x, cx<R>* w, int nvec, const VecCtx& ctx, cudaStream_t st) {
+  const PlanData<R>& d = pdata<R>(P);
+  const long long Nq = P.Nq;
+  cudaError_t e = plane_inv<R, N, true, false>(P, d, x, w, nvec, 2, 0, 4 * Nq, 2 * Nq, 6 * Nq, ctx, st);
+  if (e != cudaSuccess) return e;
+  return col<R, N, +1, 0>(d, w, 6, nvec, 6 * Nq, ctx, st);
+}
+
+template <class R, int N>
 cudaError_t transform_n(const Plan& P, int trans, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,
                         cudaStream_t st) {
   const PlanData<R>& d = pdata<R>(P);
@@ -411,6 +420,8 @@ cudaError_t handle_n(const Plan& P, int which, const cx<R>* x, cx<R>* y, int nve
   PFX cudaError_t fame::detail::fncB_n<R, NN>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&, cx<R>*,       \
                                               cx<R>*, cudaStream_t);                                               \
   PFX cudaError_t fame::detail::stencil_n<R, NN>(const Plan&, cx<R>*, cx<R>*, int, const VecCtx&, cudaStream_t);  \
+  PFX cudaError_t fame::detail::fields_inv_n<R, NN>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&,         \
+                                                    cudaStream_t);                                                 \
   PFX cudaError_t fame::detail::transform_n<R, NN>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&,     \
                                                    cudaStream_t);                                                  \
   PFX cudaError_t fame::detail::handle_n<R, NN>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&,        \

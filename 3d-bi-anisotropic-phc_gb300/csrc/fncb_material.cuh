@@ -54,11 +54,29 @@ k_vertex(const cx<R>* __restrict__ uv, cx<R>* __restrict__ h, PlanData<R> d,
   V[0] = cscale(cfma(tx, f[3 * Nq + dxm], f[3 * Nq]), R(0.5));
   V[1] = cscale(cfma(ty, f[4 * Nq + dym], f[4 * Nq]), R(0.5));
   V[2] = cscale(cfma(tz, f[5 * Nq + dzm], f[5 * Nq]), R(0.5));
+  cx<R>* o = h + vec * stride + idx;
+  if (d.fld) {  // field mode: Mh = b G, Nh = a G, J = -i g G
+    const R a = d.fld[idx], b = d.fld[Nq + idx], g = d.fld[2 * Nq + idx];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      cx<R> su = zero<R>(), sv = zero<R>();
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        if (j != i) {
+          su = cadd(su, cscale(U[j], d.gram[i * 3 + j]));
+          sv = cadd(sv, cscale(V[j], d.gram[i * 3 + j]));
+        }
+      const cx<R> tu = cadd(su, cscale(U[i], d.gram[i * 4])), tv = cadd(sv, cscale(V[i], d.gram[i * 4]));
+      // Hu_i = b sum_{j!=i} G_ij U_j + i g sum_j G_ij V_j ; Hv_i = a sum_{j!=i} G_ij V_j - i g sum_j G_ij U_j
+      o[i * Nq] = cadd(cscale(su, b), cscale(cmul_i<+1>(tv), g));
+      o[(3 + i) * Nq] = cadd(cscale(sv, a), cscale(cmul_i<-1>(tu), g));
+    }
+    return;
+  }
   const cx<R>* T = d.mat + (inst * nphase + __ldg(phase + idx)) * 27;
   const cx<R>* Nh = T;
   const cx<R>* Mh = T + 9;
   const cx<R>* J = T + 18;
-  cx<R>* o = h + vec * stride + idx;
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     cx<R> hu = zero<R>(), hv = zero<R>();
@@ -93,12 +111,30 @@ k_faceedge(cx<R>* __restrict__ uv, const cx<R>* __restrict__ h, PlanData<R> d,
   const cx<R>* tau = d.tau + inst * 3;
   const cx<R> tx = tau[0], ty = tau[1], tz = tau[2];
   // material diagonals at the corners r + {0,1}^3
-  const cx<R>* tab = d.mat + inst * nphase * 27;
-  const uint8_t* ph = phase + idx;
-  const int p000 = __ldg(ph), p100 = __ldg(ph + dxp), p010 = __ldg(ph + dyp), p001 = __ldg(ph + dzp);
-  const int p110 = __ldg(ph + dxp + dyp), p101 = __ldg(ph + dxp + dzp), p011 = __ldg(ph + dyp + dzp);
-  auto reM = [&](int p, int i) { return tab[p * 27 + 9 + i * 4].x; };
-  auto reN = [&](int p, int i) { return tab[p * 27 + i * 4].x; };
+  R m0, m1, m2, n0, n1, n2;
+  if (d.fld) {  // field mode: Re Mh_ii = b G_ii, Re Nh_ii = a G_ii
+    const R* fa = d.fld + idx;
+    const R* fb = d.fld + Nq + idx;
+    m0 = R(0.25) * d.gram[0] * (fb[0] + fb[dyp] + fb[dzp] + fb[dyp + dzp]);
+    m1 = R(0.25) * d.gram[4] * (fb[0] + fb[dxp] + fb[dzp] + fb[dxp + dzp]);
+    m2 = R(0.25) * d.gram[8] * (fb[0] + fb[dxp] + fb[dyp] + fb[dxp + dyp]);
+    n0 = R(0.5) * d.gram[0] * (fa[0] + fa[dxp]);
+    n1 = R(0.5) * d.gram[4] * (fa[0] + fa[dyp]);
+    n2 = R(0.5) * d.gram[8] * (fa[0] + fa[dzp]);
+  } else {
+    const cx<R>* tab = d.mat + inst * nphase * 27;
+    const uint8_t* ph = phase + idx;
+    const int p000 = __ldg(ph), p100 = __ldg(ph + dxp), p010 = __ldg(ph + dyp), p001 = __ldg(ph + dzp);
+    const int p110 = __ldg(ph + dxp + dyp), p101 = __ldg(ph + dxp + dzp), p011 = __ldg(ph + dyp + dzp);
+    auto reM = [&](int p, int i) { return tab[p * 27 + 9 + i * 4].x; };
+    auto reN = [&](int p, int i) { return tab[p * 27 + i * 4].x; };
+    m0 = R(0.25) * (reM(p000, 0) + reM(p010, 0) + reM(p001, 0) + reM(p011, 0));
+    m1 = R(0.25) * (reM(p000, 1) + reM(p100, 1) + reM(p001, 1) + reM(p101, 1));
+    m2 = R(0.25) * (reM(p000, 2) + reM(p100, 2) + reM(p010, 2) + reM(p110, 2));
+    n0 = R(0.5) * (reN(p000, 0) + reN(p100, 0));
+    n1 = R(0.5) * (reN(p000, 1) + reN(p010, 1));
+    n2 = R(0.5) * (reN(p000, 2) + reN(p001, 2));
+  }
   const cx<R>* hh = h + vec * stride + idx;
   cx<R>* f = uv + vec * stride + idx;
   // u'_i = m_i u_i + 1/4 (I+T_a)(I+T_b) Hu_i ; (T g)(r) = tau g(r + e)
@@ -109,12 +145,6 @@ k_faceedge(cx<R>* __restrict__ uv, const cx<R>* __restrict__ h, PlanData<R> d,
     s = cfma(cmul(ta, tb), g[da + db], s);
     return cscale(s, R(0.25));
   };
-  const R m0 = R(0.25) * (reM(p000, 0) + reM(p010, 0) + reM(p001, 0) + reM(p011, 0));
-  const R m1 = R(0.25) * (reM(p000, 1) + reM(p100, 1) + reM(p001, 1) + reM(p101, 1));
-  const R m2 = R(0.25) * (reM(p000, 2) + reM(p100, 2) + reM(p010, 2) + reM(p110, 2));
-  const R n0 = R(0.5) * (reN(p000, 0) + reN(p100, 0));
-  const R n1 = R(0.5) * (reN(p000, 1) + reN(p010, 1));
-  const R n2 = R(0.5) * (reN(p000, 2) + reN(p001, 2));
   cx<R> r[6];
   r[0] = cadd(cscale(f[0], m0), vtx2face(hh, dyp, dzp, ty, tz));
   r[1] = cadd(cscale(f[Nq], m1), vtx2face(hh + Nq, dxp, dzp, tx, tz));

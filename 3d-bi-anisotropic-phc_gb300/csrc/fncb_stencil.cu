@@ -107,6 +107,18 @@ cudaError_t launch_fncA(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const
 }
 
 template <class R>
+cudaError_t launch_fields_inv(const Plan& P, const cx<R>* x, cx<R>* w, int nvec, const VecCtx& ctx,
+                              cudaStream_t st) {
+  if (nvec <= 0) return cudaSuccess;
+  switch (P.n) {
+#define FAME_CASE(NN) case NN: return fields_inv_n<R, NN>(P, x, w, nvec, ctx, st);
+    FAME_FOR_EACH_N(FAME_CASE)
+#undef FAME_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <class R>
 cudaError_t launch_transform(const Plan& P, int trans, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,
                              cudaStream_t st) {
   if (nvec <= 0) return cudaSuccess;
@@ -156,6 +168,8 @@ cudaError_t launch_material(const Plan& P, const cx<R>* uv, cx<R>* out, int nvec
                                       cx<R>*, cudaStream_t);                                              \
   template cudaError_t launch_fncA<R>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&,             \
                                       cudaStream_t);                                                      \
+  template cudaError_t launch_fields_inv<R>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&,       \
+                                            cudaStream_t);                                                \
   template cudaError_t launch_transform<R>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&,   \
                                            cudaStream_t);                                                 \
   template cudaError_t launch_handle<R>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&,      \

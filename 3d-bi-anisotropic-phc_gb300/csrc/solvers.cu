@@ -741,11 +741,11 @@ extern "C" int fame_lanczos(fame_plan_t h, int prec, int inst, int k, double tol
 }
 
 extern "C" int fame_band_solve(fame_plan_t h, int prec, int k, double tol, int maxit, int p, double inner_tol,
-                               double* ew, double* res, long long* stats) {
+                               double* ew, void* ev, double* res, long long* stats) {
   if (!h || !ew) return FAME_ERR_BAD_ARG;
   Plan& P = h->P;
   if (prec != FAME_C128 && prec != FAME_C64) return fail(&P, FAME_ERR_BAD_ARG, "fame_band_solve: bad precision");
   std::vector<int> insts(P.nk);
   std::iota(insts.begin(), insts.end(), 0);
-  return lanczos_run(P, prec, insts, k, tol, maxit, p, nullptr, inner_tol, ew, nullptr, res, stats);
+  return lanczos_run(P, prec, insts, k, tol, maxit, p, nullptr, inner_tol, ew, (double2*)ev, res, stats);
 }

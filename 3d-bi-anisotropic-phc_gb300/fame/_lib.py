@@ -58,9 +58,12 @@ SIGNATURES = {
     "fame_apply_handle": (_i, [_vp, _i, _i, _vp, _vp, _i, _pi, _i]),
     "fame_apply_material": (_i, [_vp, _i, _vp, _vp, _i, _pi, _i]),
     "fame_lanczos": (_i, [_vp, _i, _i, _i, _d, _i, _i, _pd, _d, _pd, _vp, _pd, _pll]),
-    "fame_band_solve": (_i, [_vp, _i, _i, _d, _i, _i, _d, _pd, _pd, _pll]),
+    "fame_band_solve": (_i, [_vp, _i, _i, _d, _i, _i, _d, _pd, _vp, _pd, _pll]),
     "fame_material_blocks": (_i, [_pd, _pd, _pd]),
     "fame_jdsira": (_i, [_vp, _i, _i, _i, _d, _d, _d, _i, _i, _d, _i, _pd, _vp, _pd, _pll]),
+    "fame_plan_create_field": (_i, [C.POINTER(_vp), _i, _i, _pd, _pd, _pd, _pd]),
+    "fame_set_field": (_i, [_vp, _pd, _pd]),
+    "fame_eig_gradient": (_i, [_vp, _i, _pi, _vp, _pd, _pd, _vp, _vp, _i, _pd]),
 }
 
 

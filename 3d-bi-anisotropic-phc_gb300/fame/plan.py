@@ -74,6 +74,79 @@ class Plan:
             tens = np.stack([np.stack([covariant_blocks(m, A) for m in ci]) for ci in c])
         return cls(n, thetas, phase, tens)
 
+    @classmethod
+    def from_fields(cls, n, thetas, eps, gamma, lattice=None):
+        """Field-mode plan (fame_plan_create_field): per-vertex eps(r) I, mu = I,
+        xi = -zeta = i gamma(r) I on the n^3 vertices (x fastest)."""
+        from .setup import fcc_lattice
+        self = cls.__new__(cls)
+        self._lib = load()
+        self.n = int(n)
+        th = np.ascontiguousarray(np.asarray(thetas, dtype=np.float64).reshape(-1, 3))
+        self.nk = th.shape[0]
+        self.thetas = th
+        A = fcc_lattice() if lattice is None else np.asarray(lattice, dtype=np.float64)
+        self.lattice = np.ascontiguousarray(A.reshape(3, 3))
+        self.Nq = self.n ** 3
+        self.nphase = 1
+        self.phase = None
+        self.tensors = None
+        e, g = self._field_arrays(eps, gamma)
+        self._h = C.c_void_p()
+        pd = C.POINTER(C.c_double)
+        rc = self._lib.fame_plan_create_field(C.byref(self._h), self.n, self.nk, th.ctypes.data_as(pd),
+                                              self.lattice.ctypes.data_as(pd), e.ctypes.data_as(pd),
+                                              g.ctypes.data_as(pd))
+        check(rc, None, "fame_plan_create_field")
+        return self
+
+    def _field_arrays(self, eps, gamma):
+        def host(a):
+            if torch is not None and isinstance(a, torch.Tensor):
+                a = a.detach().cpu().numpy()
+            a = np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1))
+            if a.size != self.Nq:
+                raise ValueError("fields must hold n^3 vertex values")
+            return a
+        return host(eps), host(gamma)
+
+    def set_fields(self, eps, gamma):
+        """fame_set_field: replace the per-vertex fields of a field-mode plan."""
+        e, g = self._field_arrays(eps, gamma)
+        pd = C.POINTER(C.c_double)
+        check(self._lib.fame_set_field(self._h, e.ctypes.data_as(pd), g.ctypes.data_as(pd)), self._h,
+              "fame_set_field")
+        return self
+
+    def eig_gradient(self, ev, omega, weight=None, inst=None, out=None, accumulate=False):
+        """fame_eig_gradient: sum_v weight_v d omega_v / d(eps, gamma) at every
+        vertex.  ev: complex128 CUDA tensor (nvec, 4Nq); omega, weight (nvec,).
+        Returns (g_eps, g_gamma, xBx): FP64 CUDA tensors (Nq,) and a NumPy array."""
+        ev = ev.reshape(-1, 4 * self.Nq).contiguous()
+        if ev.dtype != torch.complex128:
+            raise TypeError("eigenvectors must be complex128")
+        nvec = ev.shape[0]
+        om = np.ascontiguousarray(np.broadcast_to(np.asarray(omega, dtype=np.float64), (nvec,)))
+        wt = np.ones(nvec) if weight is None else np.asarray(weight, dtype=np.float64)
+        wt = np.ascontiguousarray(np.broadcast_to(wt, (nvec,)))
+        if out is None:
+            g_e = torch.zeros(self.Nq, dtype=torch.float64, device=ev.device)
+            g_g = torch.zeros(self.Nq, dtype=torch.float64, device=ev.device)
+        else:
+            g_e, g_g = out
+        ip = None
+        if inst is not None:
+            ia = np.ascontiguousarray(np.broadcast_to(np.asarray(inst, dtype=np.int32), (nvec,)))
+            ip = ia.ctypes.data_as(C.POINTER(C.c_int))
+        xbx = np.zeros(nvec)
+        pd = C.POINTER(C.c_double)
+        self._stream()
+        rc = self._lib.fame_eig_gradient(self._h, nvec, ip, C.c_void_p(ev.data_ptr()), om.ctypes.data_as(pd),
+                                         wt.ctypes.data_as(pd), C.c_void_p(g_e.data_ptr()),
+                                         C.c_void_p(g_g.data_ptr()), int(bool(accumulate)), xbx.ctypes.data_as(pd))
+        check(rc, self._h, "fame_eig_gradient")
+        return g_e, g_g, xbx
+
     # -- life cycle ---------------------------------------------------------
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
@@ -240,18 +313,24 @@ class Plan:
             check(rc, self._h, "fame_jdsira")
         return dict(ew=ew, res=res, ev=ev, stats=stats, status=rc)
 
-    def band_solve(self, k, tol=1e-10, maxit=10000, p=None, prec="c64", inner_tol=1e-12):
-        """All instances at once (fame_band_solve).  Returns dict(ew, omega, res, stats, status)."""
+    def band_solve(self, k, tol=1e-10, maxit=10000, p=None, prec="c64", inner_tol=1e-12, want_vectors=False):
+        """All instances at once (fame_band_solve).  Returns dict(ew, omega, res,
+        stats, status, ev) with ev a complex128 CUDA tensor (nk, k, 4Nq) or None."""
         p = 2 * k if p is None else p
         ew = np.zeros((self.nk, k), dtype=np.float64)
         res = np.zeros((self.nk, k), dtype=np.float64)
         stats = np.zeros((self.nk, 4), dtype=np.int64)
         pd = C.POINTER(C.c_double)
+        ev = None
+        evp = None
+        if want_vectors:
+            ev = torch.empty((self.nk, k, 4 * self.Nq), dtype=torch.complex128, device="cuda")
+            evp = C.c_void_p(ev.data_ptr())
         self._stream()
         pr = L.FAME_C64 if prec in ("c64", "mixed", L.FAME_C64) else L.FAME_C128
         rc = self._lib.fame_band_solve(self._h, pr, int(k), float(tol), int(maxit), int(p), float(inner_tol),
-                                       ew.ctypes.data_as(pd), res.ctypes.data_as(pd),
+                                       ew.ctypes.data_as(pd), evp, res.ctypes.data_as(pd),
                                        stats.ctypes.data_as(C.POINTER(C.c_longlong)))
         if rc not in (L.FAME_OK, L.FAME_ERR_NOT_CONVERGED):
             check(rc, self._h, "fame_band_solve")
-        return dict(ew=ew, omega=1.0 / ew, res=res, stats=stats, status=rc)
+        return dict(ew=ew, omega=1.0 / ew, res=res, stats=stats, status=rc, ev=ev)

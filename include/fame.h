@@ -152,10 +152,11 @@ int fame_lanczos(fame_plan_t plan, int prec, int inst, int k, double tol, int ma
 /*
  * Batched band solve: fame_lanczos on every instance of the plan at once
  * (vectors of all k-points advance together; converged k-points drop out).
- * ew[nk*k], res[nk*k] (may be NULL), stats[nk*4] (may be NULL).
+ * ew[nk*k], ev (device complex128 [nk][k][4Nq], may be NULL) B-normalised
+ * Ritz vectors, res[nk*k] (may be NULL), stats[nk*4] (may be NULL).
  */
 int fame_band_solve(fame_plan_t plan, int prec, int k, double tol, int maxit, int p, double inner_tol,
-                    double* ew, double* res, long long* stats);
+                    double* ew, void* ev, double* res, long long* stats);
 
 /*
  * Interior eigenpairs by SIRA with locking: the `nev` eigenvalues theta of
@@ -176,6 +177,35 @@ int fame_band_solve(fame_plan_t plan, int prec, int k, double tol, int maxit, in
 int fame_jdsira(fame_plan_t plan, int inner_prec, int inst, int nev, double target, double shift, double tol,
                 int no_restart, int restart_dim, double inner_tol, int inner_maxit, double* ew, void* ev, double* res,
                 long long* stats);
+
+/*
+ * Plan in field mode: a per-vertex isotropic chiral medium eps(r) I, mu = I,
+ * xi = i gamma(r) I, zeta = -i gamma(r) I (the bi-isotropic form of
+ * Physical_settings_woodpile.m:76-96 with its phase constants replaced by
+ * per-vertex values).  lattice: 3x3 row-major, columns are the primitive
+ * vectors; eps, gamma [n^3] (host, x fastest), eps > 0 and eps - gamma^2 > 0.
+ * Replaces the per-vertex material placement of
+ * Material_Matrix_Generate_Mult_Point.m:38-48 for continuous fields.
+ */
+int fame_plan_create_field(fame_plan_t* plan, int n, int nk, const double* theta, const double* lattice,
+                           const double* eps, const double* gamma);
+/* Replace the fields of a field-mode plan (same constraints). */
+int fame_set_field(fame_plan_t plan, const double* eps, const double* gamma);
+
+/*
+ * Backward entry: gradient of a weighted sum of eigenfrequencies,
+ *   g_eps[r] = sum_v weight[v] d omega_v / d eps(r),  likewise g_gamma,
+ * by the Hellmann-Feynman form d omega = omega x^H dB x / (x^H B x) evaluated
+ * vertex by vertex in FP64.  x: device complex128 [nvec][4Nq] eigenvectors of
+ * fncA x = (1/omega) fncB x (any normalisation), vector v of instance inst[v]
+ * (inst NULL: v % nk); omega, weight [nvec] host; g_eps, g_gamma [n^3] device
+ * FP64, overwritten (accumulate = 0) or added to; xbx [nvec] host (may be
+ * NULL) receives x^H B x.  Field-mode plans only.  For a degenerate cluster
+ * give every member the same weight (the trace is what is differentiable).
+ * No counterpart in the reference.
+ */
+int fame_eig_gradient(fame_plan_t plan, int nvec, const int* inst, const void* x, const double* omega,
+                      const double* weight, double* g_eps, double* g_gamma, int accumulate, double* xbx);
 
 /*
  * Covariant material blocks of one phase: invert the 6x6 constitutive block

@@ -30,6 +30,8 @@ __all__ = [
     "interp_material_vertex", "MaterialOps", "fncA", "fncB", "pcg_matlab",
     "fncinvB", "lanczos", "eigen_restoration", "evaluate_error",
     "BandProblem", "build_problem", "woodpile_phases", "fft_workers",
+    "field_diagonals", "build_problem_field", "material_quad_coeffs", "field_gradient",
+    "chiral_noise_field",
 ]
 
 _W = max(1, min(8, os.cpu_count() or 1))
@@ -714,3 +716,134 @@ def build_problem(n, wave_vec=None, thetas=None, gamma=0.2, eps_in=13.0, width=0
     Nint, Mint, Jint = interp_material_vertex(dims, thetas, Nv, Mv, Jv)
     return BandProblem(dims, tuple(thetas), svd, make_handles(svd), MaterialOps(Nint, Mint, Jint),
                        inside, blocks)
+
+
+# --------------------------------------------------------------------------
+# Per-vertex chiral fields and the eigenfrequency gradient (no reference
+# counterpart: the reference places two-phase materials only; these restate
+# the same assembly for per-vertex values and differentiate it)
+# --------------------------------------------------------------------------
+def field_diagonals(eps, gam, A=None):
+    """Per-vertex covariant diagonals of ``eps I, mu = I, xi = i gamma I,
+    zeta = -i gamma I``: ``material_blocks`` of each vertex in closed form,
+    ``N = a G``, ``M = eps a G``, ``J = -i gamma a G`` with ``a = 1/(eps - gamma^2)``
+    and ``G = A' A``.  Returns the 3x3 nested lists ``(Nv, Mv, Jv)`` that
+    ``interp_material_vertex`` takes, and ``(a, b, g, G)``."""
+    A = fcc_lattice() if A is None else A
+    eps = np.asarray(eps, dtype=np.float64)
+    gam = np.asarray(gam, dtype=np.float64)
+    a = 1.0 / (eps - gam * gam)
+    b = eps * a
+    g = gam * a
+    G = A.T @ A
+    Nv = [[a * G[i, j] + 0j for j in range(3)] for i in range(3)]
+    Mv = [[b * G[i, j] + 0j for j in range(3)] for i in range(3)]
+    Jv = [[-1j * g * G[i, j] for j in range(3)] for i in range(3)]
+    return (Nv, Mv, Jv), (a, b, g, G)
+
+
+def build_problem_field(n, eps, gam, wave_vec=None, thetas=None, A=None) -> BandProblem:
+    """``build_problem`` with per-vertex fields in place of the two phases."""
+    A = fcc_lattice() if A is None else A
+    dims = Dims(n, n, n)
+    if thetas is None:
+        thetas = thetas_from_k(wave_vec, A)
+    (Nv, Mv, Jv), _ = field_diagonals(eps, gam, A)
+    svd = svd_matrix_generate(dims, thetas)
+    Nint, Mint, Jint = interp_material_vertex(dims, thetas, Nv, Mv, Jv)
+    return BandProblem(dims, tuple(thetas), svd, make_handles(svd), MaterialOps(Nint, Mint, Jint),
+                       np.zeros(dims.Nq, dtype=bool), [])
+
+
+def material_quad_coeffs(dims: Dims, thetas, u, v):
+    """Adjoint of ``interp_material_vertex``: per-vertex coefficient arrays
+    ``cN[i][j]``, ``cM[i][j]``, ``cJ[i][j]`` such that, for per-vertex
+    diagonals ``Nv``, ``Mv``, ``Jv``,
+
+        u' M_int u = sum Re(Mv_ij * cM_ij),   v' N_int v = sum Re(Nv_ij * cN_ij),
+        v' J_int u = sum Jv_ij * cJ_ij.
+
+    Each assembled term ``L diag(A) R`` contributes ``conj(L' y_i) .* (R y_j)``;
+    the factors are those of ``interp_material_vertex`` literally."""
+    N = dims.Nq
+    I = _I(N)
+    C = [shift_diff(dims, thetas, d) for d in range(3)]
+    CH = [c.conj().T.tocsr() for c in C]
+    U = [u[i * N:(i + 1) * N] for i in range(3)]
+    V = [v[i * N:(i + 1) * N] for i in range(3)]
+
+    def k_of(i):
+        return [d for d in range(3) if d != i]
+
+    def term(Lfac, Rfac, yi, yj):
+        return np.conj(Lfac.conj().T @ yi) * (Rfac @ yj)
+
+    cN = [[None] * 3 for _ in range(3)]
+    cM = [[None] * 3 for _ in range(3)]
+    cJ = [[None] * 3 for _ in range(3)]
+    for i in range(3):
+        for j in range(3):
+            if i != j:
+                cN[i][j] = term(0.25 * (2 * I + C[i]), 2 * I + CH[j], V[i], V[j])
+            else:
+                cN[i][i] = 0.5 * (np.conj(V[i]) * V[i] + term(I + C[i], I + CH[i], V[i], V[i]))
+    for i in range(3):
+        k = k_of(i)
+        t1, t2 = (I + C[k[0]]), (I + C[k[1]])
+        for j in range(3):
+            if i == j:
+                cM[i][i] = 0.25 * (np.conj(U[i]) * U[i] + term(t1, t1.conj().T, U[i], U[i])
+                                   + term(t2, t2.conj().T, U[i], U[i])
+                                   + term(t1 @ t2, t2.conj().T @ t1.conj().T, U[i], U[i]))
+            else:
+                l = k_of(j)
+                cM[i][j] = term((1.0 / 16) * (2 * I + C[k[0]]) @ (2 * I + C[k[1]]),
+                                (2 * I + CH[l[1]]) @ (2 * I + CH[l[0]]), U[i], U[j])
+    for i in range(3):
+        for j in range(3):
+            k = k_of(j)
+            cJ[i][j] = term(0.125 * (2 * I + C[i]), (2 * I + CH[k[1]]) @ (2 * I + CH[k[0]]), V[i], U[j])
+    return cN, cM, cJ
+
+
+def field_gradient(prob: BandProblem, x, omega, eps, gam, A=None):
+    """FP64 reference gradient of one eigenfrequency with respect to the
+    per-vertex fields: ``d omega/dp = omega x' (dB/dp) x / (x' B x)`` with
+    ``x' B x = u' M_int u + v' N_int v + 2 Re(v' J_int u)`` (``fncB.m:3-6``,
+    ``u = Pr x1``, ``v = Qr x2``), differentiated through the literal
+    assembly via ``material_quad_coeffs``.  Returns ``(g_eps, g_gamma, xBx)``."""
+    A = fcc_lattice() if A is None else A
+    N = prob.dims.Nq
+    x = np.asarray(x, dtype=np.complex128)
+    u = prob.fnc.Pr(x[:2 * N])
+    v = prob.fnc.Qr(x[2 * N:])
+    cN, cM, cJ = material_quad_coeffs(prob.dims, prob.thetas, u, v)
+    (_, _, _), (a, b, g, G) = field_diagonals(eps, gam, A)
+    eps = np.asarray(eps, dtype=np.float64)
+    gam = np.asarray(gam, dtype=np.float64)
+    SN = sum(G[i, j] * cN[i][j].real for i in range(3) for j in range(3))
+    SM = sum(G[i, j] * cM[i][j].real for i in range(3) for j in range(3))
+    SJ = sum(G[i, j] * cJ[i][j].imag for i in range(3) for j in range(3))
+    xbx = float(np.sum(a * SN + b * SM + 2.0 * g * SJ))
+    a2 = a * a
+    dq_de = -a2 * SN - gam * gam * a2 * SM - 2.0 * gam * a2 * SJ
+    dq_dg = 2.0 * gam * a2 * SN + 2.0 * eps * gam * a2 * SM + 2.0 * a * (1.0 + 2.0 * gam * gam * a) * SJ
+    s = omega / xbx
+    return s * dq_de, s * dq_dg, xbx
+
+
+def chiral_noise_field(n, seed=0, sigma=2.0, slope=8.0, eps_lo=1.0, eps_span=12.0, gamma_max=0.2):
+    """Seeded smooth random medium on the n^3 vertices: s = sigmoid(slope *
+    blur(N(0,1), sigma voxels)) with a periodic Gaussian blur (normalised to
+    zero mean and unit standard deviation before the sigmoid), eps = eps_lo + eps_span s,
+    gamma = gamma_max s.  Returns (eps, gamma), x fastest."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal((n, n, n))  # [z, y, x]
+    k = np.fft.fftfreq(n) * 2 * np.pi
+    kz, ky, kx = np.meshgrid(k, k, k, indexing="ij")
+    filt = np.exp(-0.5 * sigma * sigma * (kx ** 2 + ky ** 2 + kz ** 2))
+    sm = np.real(np.fft.ifftn(np.fft.fftn(w) * filt))
+    sm = (sm - sm.mean()) / sm.std()
+    s = 1.0 / (1.0 + np.exp(-slope * sm))
+    s = s.reshape(-1)
+    return eps_lo + eps_span * s, gamma_max * s
