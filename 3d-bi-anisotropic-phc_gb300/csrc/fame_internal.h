@@ -115,6 +115,10 @@ cudaError_t launch_transform(const Plan& P, int trans, const cx<R>* x, cx<R>* y,
 template <class R>
 cudaError_t launch_handle(const Plan& P, int which, const cx<R>* x, cx<R>* y, int nvec,
                           const VecCtx& ctx, cx<R>* w0, cudaStream_t st);
+// Material stencil in place on periodic-frame 6-field vectors w (stride 6*Nq),
+// scratch h of the same size: w <- [M J^H; J N] w.
+template <class R>
+cudaError_t launch_stencil(const Plan& P, cx<R>* w, cx<R>* h, int nvec, const VecCtx& ctx, cudaStream_t st);
 // Material operator alone on spatial 6-field vectors (periodic frame, no S):
 // [u'; v'] = [M J^H; J N] [u; v], the middle factor of fncB.
 template <class R>

@@ -107,6 +107,12 @@ cudaError_t launch_fncA(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const
 }
 
 template <class R>
+cudaError_t launch_stencil(const Plan& P, cx<R>* w, cx<R>* h, int nvec, const VecCtx& ctx, cudaStream_t st) {
+  if (nvec <= 0) return cudaSuccess;
+  return stencil<R>(P, w, h, nvec, ctx, st);
+}
+
+template <class R>
 cudaError_t launch_fields_inv(const Plan& P, const cx<R>* x, cx<R>* w, int nvec, const VecCtx& ctx,
                               cudaStream_t st) {
   if (nvec <= 0) return cudaSuccess;
@@ -170,6 +176,7 @@ cudaError_t launch_material(const Plan& P, const cx<R>* uv, cx<R>* out, int nvec
                                       cudaStream_t);                                                      \
   template cudaError_t launch_fields_inv<R>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&,       \
                                             cudaStream_t);                                                \
+  template cudaError_t launch_stencil<R>(const Plan&, cx<R>*, cx<R>*, int, const VecCtx&, cudaStream_t); \
   template cudaError_t launch_transform<R>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&,   \
                                            cudaStream_t);                                                 \
   template cudaError_t launch_handle<R>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&,      \

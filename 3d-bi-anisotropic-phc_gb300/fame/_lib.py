@@ -64,6 +64,7 @@ SIGNATURES = {
     "fame_plan_create_field": (_i, [C.POINTER(_vp), _i, _i, _pd, _pd, _pd, _pd]),
     "fame_set_field": (_i, [_vp, _pd, _pd]),
     "fame_eig_gradient": (_i, [_vp, _i, _pi, _vp, _pd, _pd, _vp, _vp, _i, _pd]),
+    "fame_restore": (_i, [_vp, _i, _pi, _vp, _pd, _vp, _vp, _pd, _pd, _pd, _i]),
 }
 
 

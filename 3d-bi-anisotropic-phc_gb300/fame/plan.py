@@ -147,6 +147,35 @@ class Plan:
         check(rc, self._h, "fame_eig_gradient")
         return g_e, g_g, xbx
 
+    def restore(self, ev, omega, inst=None, want_fields=True, outside_only=False):
+        """fame_restore: E, H fields (Eigen_Restoration_Chiral_no_inv.m), the
+        ORGSEP residual (EvaluteError_Chiral_no_inv.m:19) and max |e_c|, |h_c|
+        (Fig6cd_plot_max_field.m).  Returns dict(E, H, res_orgsep, max_e, max_h)."""
+        ev = ev.reshape(-1, 4 * self.Nq).contiguous()
+        if ev.dtype != torch.complex128:
+            raise TypeError("eigenvectors must be complex128")
+        nvec = ev.shape[0]
+        om = np.ascontiguousarray(np.broadcast_to(np.asarray(omega, dtype=np.float64), (nvec,)))
+        E = H = None
+        if want_fields:
+            E = torch.empty((nvec, 3 * self.Nq), dtype=torch.complex128, device=ev.device)
+            H = torch.empty_like(E)
+        res = np.zeros(nvec)
+        me = np.zeros(nvec)
+        mh = np.zeros(nvec)
+        ip = None
+        if inst is not None:
+            ia = np.ascontiguousarray(np.broadcast_to(np.asarray(inst, dtype=np.int32), (nvec,)))
+            ip = ia.ctypes.data_as(C.POINTER(C.c_int))
+        pd = C.POINTER(C.c_double)
+        self._stream()
+        rc = self._lib.fame_restore(self._h, nvec, ip, C.c_void_p(ev.data_ptr()), om.ctypes.data_as(pd),
+                                    C.c_void_p(E.data_ptr()) if E is not None else None,
+                                    C.c_void_p(H.data_ptr()) if H is not None else None, res.ctypes.data_as(pd),
+                                    me.ctypes.data_as(pd), mh.ctypes.data_as(pd), int(bool(outside_only)))
+        check(rc, self._h, "fame_restore")
+        return dict(E=E, H=H, res_orgsep=res, max_e=me, max_h=mh)
+
     # -- life cycle ---------------------------------------------------------
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -179,6 +179,23 @@ int fame_jdsira(fame_plan_t plan, int inner_prec, int inst, int nev, double targ
                 long long* stats);
 
 /*
+ * Eigenvector restoration and checks for FP64 eigenpairs x (device complex128
+ * [nvec][4Nq], vector v of instance inst[v], inst NULL: v % nk) with
+ * frequencies omega[nvec] (host):
+ *   E, H (device complex128 [nvec][3Nq] each, may be NULL): the fields
+ *     [e; h] = -1i*[N J; J' M]*[Qr(x2); Pr(x1)]
+ *     (Eigen_Restoration_Chiral_no_inv.m:3-25);
+ *   res_orgsep[nvec] (host, may be NULL): the ORGSEP residual
+ *     ||[N J; J' M]*[C'*h; -C*e] - 1i*omega*[e; h]|| with the explicit curl
+ *     C of @DistOp/C.m (EvaluteError_Chiral_no_inv.m:19);
+ *   max_e, max_h[nvec] (host, may be NULL): max over components of |e_c| and
+ *     |h_c|, at every vertex or (outside_only != 0) at vertices of phase id 0
+ *     only (Fig6cd_plot_max_field.m:58-69).
+ */
+int fame_restore(fame_plan_t plan, int nvec, const int* inst, const void* x, const double* omega, void* E, void* H,
+                 double* res_orgsep, double* max_e, double* max_h, int outside_only);
+
+/*
  * Plan in field mode: a per-vertex isotropic chiral medium eps(r) I, mu = I,
  * xi = i gamma(r) I, zeta = -i gamma(r) I (the bi-isotropic form of
  * Physical_settings_woodpile.m:76-96 with its phase constants replaced by
