@@ -157,6 +157,33 @@ def sphere_inside(P: np.ndarray, radius: float, A: np.ndarray | None = None,
     return best < radius
 
 
+def tetra_inside(P: np.ndarray, edge: float, A: np.ndarray | None = None,
+                 center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Regular tetrahedron of edge length `edge` centred at `center` (vertices
+    along (1,1,1), (1,-1,-1), (-1,1,-1), (-1,-1,1)), with all periodic images.
+    A point is inside when, for each face, it lies on the same side as the
+    opposite vertex (the four half-space tests of
+    subroutines/Material_Locate_Isofunction.m:38-90; within 1e-8 of a face
+    counts as inside)."""
+    A = fcc_lattice() if A is None else A
+    s = edge / (2.0 * math.sqrt(2.0))
+    base = s * np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], dtype=np.float64)
+    inside = np.zeros(P.shape[0], dtype=bool)
+    for i in (-1, 0, 1):
+        for j in (-1, 0, 1):
+            for k in (-1, 0, 1):
+                verts = base + np.asarray(center) + A @ np.array([i, j, k], dtype=np.float64)
+                ok = np.ones(P.shape[0], dtype=bool)
+                for f in range(4):
+                    a, b, c = [verts[t] for t in range(4) if t != f]
+                    nrm = np.cross(b - a, c - a)
+                    dp = (a - P) @ nrm
+                    dq = float(np.dot(a - verts[f], nrm))
+                    ok &= (np.abs(dp) < 1e-8) | (dp * dq > 0)
+                inside |= ok
+    return inside
+
+
 def constitutive(eps, mu, xi, zeta) -> np.ndarray:
     """The 6x6 block [eps xi; zeta mu] (complex)."""
     return np.block([[np.asarray(eps), np.asarray(xi)], [np.asarray(zeta), np.asarray(mu)]]).astype(np.complex128)

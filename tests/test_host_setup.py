@@ -62,3 +62,22 @@ def test_sphere_periodic_images():
     frac = m.mean()
     vol = 4 / 3 * np.pi * 0.25 ** 3 / abs(np.linalg.det(A))
     assert abs(frac - vol) < 0.05
+
+
+def test_tetra_inside_matches_oracle_isofun():
+    """fame.tetra_inside (periodic images) against the oracle's four
+    half-space test (Material_Locate_Isofunction.m) applied to each image."""
+    import oracle as O
+    A = fame.fcc_lattice()
+    P = fame.vertex_positions(12, A)
+    edge = 0.5
+    s = edge / (2.0 * np.sqrt(2.0))
+    base = s * np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], dtype=np.float64)
+    ref = np.zeros(P.shape[0], dtype=bool)
+    for i in (-1, 0, 1):
+        for j in (-1, 0, 1):
+            for k in (-1, 0, 1):
+                ref |= O.tetra_isofun(P, base + A @ np.array([i, j, k], dtype=np.float64))
+    got = fame.tetra_inside(P, edge, A)
+    assert got.sum() > 0
+    assert np.array_equal(got, ref)
