@@ -219,6 +219,7 @@ int set_field(Plan& P, const double* eps, const double* gam) {
   P.d32.pc = nullptr;
   cudaFree(P.d_mat_avg);
   P.d_mat_avg = nullptr;
+  free_graphs(P);  // captured CG iterations hold the preconditioner's address
   return FAME_OK;
 }
 

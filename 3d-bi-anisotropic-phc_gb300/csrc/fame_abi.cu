@@ -316,6 +316,7 @@ int fame_plan_destroy(fame_plan_t h) {
   cudaFree(P.d_stage);
   cudaFree(P.d_mat_avg);
   cudaFree(P.d_eps_gam);
+  free_graphs(P);
   if (P.h_ring) cudaFreeHost(P.h_ring);
   free_workspaces(P);
   delete h;
@@ -328,6 +329,9 @@ int fame_set_option(fame_plan_t h, int option, double value) {
   switch (option) {
     case FAME_OPT_PRECOND:
       P.opt_precond = value != 0.0;
+      return FAME_OK;
+    case FAME_OPT_GRAPH:
+      P.opt_graph = value != 0.0;
       return FAME_OK;
     case FAME_OPT_TOL32:
       if (!(value > 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: tol32 in (0,1)");

@@ -41,6 +41,14 @@ template <class R> struct PlanData {
   R gram[9] = {};
 };
 
+// Instantiated CUDA graphs of a plan, keyed by everything a captured launch
+// sequence depends on (precision, sizes, device pointers).
+struct GraphEntry {
+  std::vector<uintptr_t> key;
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long nodes = 0;  // kernel nodes (launch accounting)
+};
+
 struct Plan {
   int n = 0;         // cubic grid n1 = n2 = n3 = n
   long long Nq = 0;  // n^3
@@ -51,6 +59,7 @@ struct Plan {
   // options (fame_set_option)
   int opt_precond = 1;                // CG on B preconditioned by the averaged-medium B0^{-1}
   double opt_tol32 = 1e-6;            // complex64 CG tolerance of the first refinement round
+  int opt_graph = 1;                  // replay CG iterations from captured CUDA graphs
   std::vector<double> theta;          // [nk][3]
   std::vector<double> sigma_min;      // [nk] smallest curl singular value sqrt(min |L|^2)
   std::vector<double> mat_avg;        // [nk][27][2] volume-averaged Herm(N) | Herm(M) | J
@@ -82,7 +91,18 @@ struct Plan {
   // would synchronise the stream)
   char* h_ring = nullptr;
   size_t ring_pos = 0;
+  // captured launch sequences (graph.cu)
+  cudaStream_t cap_stream = nullptr;
+  std::vector<GraphEntry> graphs;
 };
+
+// Replay the launch sequence that `issue(stream)` enqueues, from a graph cached
+// under `key` (captured on first use on a private stream), on the plan's
+// stream.  Returns cudaErrorNotSupported when capture is not possible, in
+// which case the caller issues the sequence directly.
+template <class F>
+cudaError_t graph_replay(Plan& P, const std::vector<uintptr_t>& key, F&& issue);
+void free_graphs(Plan& P);
 
 // Asynchronous small upload through the plan's pinned ring (stream-ordered).
 cudaError_t h2d_async(Plan& P, void* dst, const void* src, size_t bytes);

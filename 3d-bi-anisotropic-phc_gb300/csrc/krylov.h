@@ -27,7 +27,7 @@ template <class R>
 cudaError_t cg_p(cx<R>* p, const cx<R>* r, long long len, long long stride, int nvec, const double* beta,
                  const int* active, cudaStream_t st);
 cudaError_t cg_scalars(int stage, int nvec, const double2* dot, double* rho, double* alpha, double* beta,
-                       const double* tol2b2, int* active, int* iters, double* res2, int it, cudaStream_t st);
+                       const double* tol2b2, int* active, int* iters, double* res2, cudaStream_t st);
 template <class R>
 cudaError_t block_rot(const cx<R>* in, cx<R>* out, long long len, long long ld, int p, int k, const double* U,
                       cudaStream_t st);

@@ -167,12 +167,16 @@ __global__ void k_cg_p(cx<R>* __restrict__ p, const cx<R>* __restrict__ r, long 
 
 // Per-vector CG scalars.  stage 0: alpha = rho/Re(pq); stage 1: convergence
 // test on rho_new and beta = rho_new/rho.
+// iters[v] counts the completed iterations of vector v on the device (so an
+// iteration needs no host-side argument and can be replayed from a graph);
+// a negative count flags breakdown at that iteration.
 __global__ void k_cg_scalars(int stage, int nvec, const double2* __restrict__ dot, double* __restrict__ rho,
                              double* __restrict__ alpha, double* __restrict__ beta,
                              const double* __restrict__ tol2b2, int* __restrict__ active,
-                             int* __restrict__ iters, double* __restrict__ res2, int it) {
+                             int* __restrict__ iters, double* __restrict__ res2) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nvec || !active[v]) return;
+  const int it = iters[v] + 1;
   if (stage == 0) {
     const double pq = dot[v].x;
     alpha[v] = (pq != 0.0 && isfinite(pq)) ? rho[v] / pq : 0.0;
@@ -396,10 +400,10 @@ cudaError_t cg_p(cx<R>* p, const cx<R>* r, long long len, long long stride, int 
 }
 
 cudaError_t cg_scalars(int stage, int nvec, const double2* dot, double* rho, double* alpha, double* beta,
-                       const double* tol2b2, int* active, int* iters, double* res2, int it, cudaStream_t st) {
+                       const double* tol2b2, int* active, int* iters, double* res2, cudaStream_t st) {
   FAME_LAUNCHED(1);
   k_cg_scalars<<<(nvec + 127) / 128, 128, 0, st>>>(stage, nvec, dot, rho, alpha, beta, tol2b2, active, iters,
-                                                    res2, it);
+                                                    res2);
   return cudaGetLastError();
 }
 

@@ -10,6 +10,7 @@
 #include <numeric>
 #include <vector>
 
+#include "graph_impl.h"
 #include "krylov.h"
 #include "linalg_host.h"
 
@@ -131,25 +132,52 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
   } else {
     FAME_CK(cudaMemcpyAsync(p, b, vb, cudaMemcpyDeviceToDevice, st), "pcg init");
   }
-  const int chk = 4;
-  bool any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
-  for (int it = 1; it <= maxit && any; ++it) {
-    FAME_CK(launch_fncB<R>(P, p, q, nvec, ctx, w0, w1, st), "pcg fncB");
-    FAME_CK(dot_batched<R>(p, L, 0, 1, q, L, L, nvec, S.dot, part, nblk, S.active, st), "pcg dot");
-    FAME_CK(cg_scalars(0, nvec, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active, S.iters, S.res2, it, st), "pcg");
+  // One CG iteration: every kernel reads its scalars and active flags from
+  // the device, so a block of iterations is a fixed launch sequence that is
+  // captured once per (sizes, pointers) and replayed from a CUDA graph.
+  auto iteration = [&](cudaStream_t cs) -> cudaError_t {
+    cudaError_t e2 = launch_fncB<R>(P, p, q, nvec, ctx, w0, w1, cs);
+    if (e2 == cudaSuccess) e2 = dot_batched<R>(p, L, 0, 1, q, L, L, nvec, S.dot, part, nblk, S.active, cs);
+    if (e2 == cudaSuccess)
+      e2 = cg_scalars(0, nvec, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active, S.iters, S.res2, cs);
     if (pre) {
-      FAME_CK(pcg_update<R>(P, x, r, z, p, q, nvec, ctx, S.alpha, part, nblkv, st), "pcg update");
-      FAME_CK(dot_final(part, nblkv, nvec, S.dot, st), "pcg update");
-    } else {
-      FAME_CK(cg_xr_dot<R>(x, r, p, q, L, L, nvec, S.alpha, S.active, S.dot, part, nblk, st), "pcg update");
+      if (e2 == cudaSuccess) e2 = pcg_update<R>(P, x, r, z, p, q, nvec, ctx, S.alpha, part, nblkv, cs);
+      if (e2 == cudaSuccess) e2 = dot_final(part, nblkv, nvec, S.dot, cs);
+    } else if (e2 == cudaSuccess) {
+      e2 = cg_xr_dot<R>(x, r, p, q, L, L, nvec, S.alpha, S.active, S.dot, part, nblk, cs);
     }
-    FAME_CK(cg_scalars(1, nvec, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active, S.iters, S.res2, it, st), "pcg");
-    FAME_CK(cg_p<R>(p, pre ? z : r, L, L, nvec, S.beta, S.active, st), "pcg update");
-    if (it % chk == 0 || it == maxit) {
-      FAME_CK(cudaMemcpyAsync(act.data(), S.active, sizeof(int) * nvec, cudaMemcpyDeviceToHost, st), "pcg check");
-      FAME_CK(cudaStreamSynchronize(st), "pcg check");
-      any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
+    if (e2 == cudaSuccess)
+      e2 = cg_scalars(1, nvec, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active, S.iters, S.res2, cs);
+    if (e2 == cudaSuccess) e2 = cg_p<R>(p, pre ? z : r, L, L, nvec, S.beta, S.active, cs);
+    return e2;
+  };
+  const int chk = 4;
+  const std::vector<uintptr_t> gkey = {sizeof(R), (uintptr_t)nvec, (uintptr_t)pre, (uintptr_t)chk, (uintptr_t)P.n,
+                                       (uintptr_t)p, (uintptr_t)q, (uintptr_t)x, (uintptr_t)r, (uintptr_t)z,
+                                       (uintptr_t)w0, (uintptr_t)w1, (uintptr_t)s, (uintptr_t)part,
+                                       (uintptr_t)d_inst, (uintptr_t)nblk, (uintptr_t)nblkv,
+                                       sizeof(R) == 4 ? (uintptr_t)P.d32.pc : (uintptr_t)P.d64.pc};
+  bool use_graph = P.opt_graph != 0;
+  bool any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
+  for (int it = 1; it <= maxit && any; it += chk) {
+    const int nit = std::min(chk, maxit - it + 1);
+    bool done = false;
+    if (use_graph && nit == chk) {
+      cudaError_t ge = graph_replay(P, gkey, [&](cudaStream_t cs) -> cudaError_t {
+        for (int i = 0; i < chk; ++i) {
+          cudaError_t e2 = iteration(cs);
+          if (e2 != cudaSuccess) return e2;
+        }
+        return cudaSuccess;
+      });
+      if (ge == cudaSuccess) done = true;
+      else use_graph = false;  // capture unavailable: issue directly from now on
     }
+    if (!done)
+      for (int i = 0; i < nit; ++i) FAME_CK(iteration(st), "pcg iteration");
+    FAME_CK(cudaMemcpyAsync(act.data(), S.active, sizeof(int) * nvec, cudaMemcpyDeviceToHost, st), "pcg check");
+    FAME_CK(cudaStreamSynchronize(st), "pcg check");
+    any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
   }
   std::vector<int> its(nvec);
   std::vector<double> r2(nvec);

@@ -79,8 +79,10 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *                     inverse B0^{-1} [1]; 0 gives the reference's
  *                     unpreconditioned pcg of fncinvB.m.
  *   FAME_OPT_TOL32    complex64 CG tolerance of the first refinement round of
- *                     the mixed-precision B^{-1} [1e-6]. */
-enum fame_option { FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1 };
+ *                     the mixed-precision B^{-1} [1e-6].
+ *   FAME_OPT_GRAPH    replay blocks of CG iterations from CUDA graphs captured
+ *                     on first use [1]; 0 launches every kernel directly. */
+enum fame_option { FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2 };
 int fame_set_option(fame_plan_t plan, int option, double value);
 int fame_sync(fame_plan_t plan);
 const char* fame_last_error(fame_plan_t plan);

@@ -159,3 +159,25 @@ def test_errors(cuda, fame_lib):
     assert e.value.code == 1
     empty = torch.zeros((0, 4 * P.Nq), dtype=torch.complex128, device="cuda")
     assert P.plan.apply_B(empty).shape == (0, 4 * P.Nq)
+
+
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_cg_graph_replay_matches_direct_launches(cuda, fame_lib, prec):
+    """Blocks of CG iterations replayed from captured CUDA graphs give the same
+    iterates as launching every kernel directly (same kernels, same order)."""
+    pr = Pair(8, nk=2, seed=21)
+    rng = np.random.default_rng(5)
+    b = rng.standard_normal((3, 4 * pr.Nq)) + 1j * rng.standard_normal((3, 4 * pr.Nq))
+    import torch
+    bt = torch.as_tensor(b).to(torch.complex128 if prec == "c128" else torch.complex64).cuda()
+    tol = 1e-10 if prec == "c128" else 1e-5
+    out = {}
+    for g in (1, 0):
+        pr.plan.set_option("graph", g)
+        y, its, rr = pr.plan.apply_Binv(bt, tol=tol, maxit=2000)
+        y2, its2, _ = pr.plan.apply_Binv(bt, tol=tol, maxit=2000)
+        assert torch.equal(y, y2) and np.array_equal(its, its2)  # second call replays the cached graph
+        out[g] = (y.cpu().numpy(), its.copy(), rr.copy())
+    pr.plan.set_option("graph", 1)
+    assert np.array_equal(out[1][1], out[0][1])
+    assert np.array_equal(out[1][0], out[0][0])
