@@ -1,0 +1,132 @@
+// Autotuner of the fncB launch sequence: times the candidate launch
+// parameters on the plan's own grid, instances and batch width and keeps the
+// fastest per (precision, batch width).  Knobs:
+//   chunk        vectors per launch sequence (whole batch, 1/2, 1/4, 1/8):
+//                smaller sub-batches keep the six-field intermediates in L2
+//                at the cost of smaller grids;
+//   stencil_tpb  threads per block of the two stencil kernels (128/256/512).
+// No counterpart in the reference.
+#include <algorithm>
+#include <vector>
+
+#include "fame_internal.h"
+
+namespace fame {
+
+TuneEntry tune_for(const Plan& P, int prec, int nvec) {
+  for (const TuneEntry& t : P.tune)
+    if (t.prec == prec && t.nvec == nvec) return t;
+  TuneEntry d;
+  d.prec = prec;
+  d.nvec = nvec;
+  return d;
+}
+
+static void put_tune(Plan& P, const TuneEntry& t) {
+  for (TuneEntry& u : P.tune)
+    if (u.prec == t.prec && u.nvec == t.nvec) {
+      u = t;
+      return;
+    }
+  P.tune.push_back(t);
+}
+
+template <class R>
+static int autotune_prec(Plan& P, int nvec, int reps, TuneEntry* best_out) {
+  cudaStream_t st = P.stream;
+  const long long L = 4 * P.Nq;
+  cudaError_t e;
+  cx<R>* x = (cx<R>*)workspace(P, 60, sizeof(cx<R>) * L * nvec, &e);
+  if (e != cudaSuccess) return cuda_fail(&P, e, "autotune buffers");
+  cx<R>* y = (cx<R>*)workspace(P, 61, sizeof(cx<R>) * L * nvec, &e);
+  if (e != cudaSuccess) return cuda_fail(&P, e, "autotune buffers");
+  e = cudaMemsetAsync(x, 0x3c, sizeof(cx<R>) * L * nvec, st);  // finite, normal values
+  if (e == cudaSuccess) e = ensure_work(P, nvec);
+  if (e != cudaSuccess) return cuda_fail(&P, e, "autotune setup");
+  cx<R>* w0 = (cx<R>*)P.d_work;
+  cx<R>* w1 = w0 + (size_t)nvec * 6 * P.Nq;
+  VecCtx ctx;
+  ctx.nk = P.nk;
+  std::vector<int> chunks;
+  for (int div : {1, 2, 4, 8}) {
+    const int c = (nvec + div - 1) / div;
+    if (c >= 1 && std::find(chunks.begin(), chunks.end(), c) == chunks.end()) chunks.push_back(c);
+  }
+  const int prec = sizeof(R) == 4 ? FAME_C64 : FAME_C128;
+  const TuneEntry saved = tune_for(P, prec, nvec);
+  cudaEvent_t ev[2];
+  cudaEventCreate(&ev[0]);
+  cudaEventCreate(&ev[1]);
+  TuneEntry best;
+  best.us = 1e300;
+  for (int c : chunks)
+    for (int tpb : {128, 256, 512}) {
+      TuneEntry t;
+      t.prec = prec;
+      t.nvec = nvec;
+      t.chunk = c == nvec ? 0 : c;
+      t.stencil_tpb = tpb;
+      put_tune(P, t);
+      e = launch_fncB<R>(P, x, y, nvec, ctx, w0, w1, st);  // warm-up
+      std::vector<float> ms;
+      for (int r = 0; r < reps && e == cudaSuccess; ++r) {
+        cudaEventRecord(ev[0], st);
+        e = launch_fncB<R>(P, x, y, nvec, ctx, w0, w1, st);
+        cudaEventRecord(ev[1], st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+        float m = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&m, ev[0], ev[1]);
+        ms.push_back(m);
+      }
+      if (e != cudaSuccess) {
+        cudaEventDestroy(ev[0]);
+        cudaEventDestroy(ev[1]);
+        put_tune(P, saved);
+        return cuda_fail(&P, e, "autotune");
+      }
+      std::sort(ms.begin(), ms.end());
+      t.us = 1e3 * double(ms[ms.size() / 2]);
+      if (t.us < best.us) best = t;
+    }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  put_tune(P, best);
+  *best_out = best;
+  return FAME_OK;
+}
+
+}  // namespace fame
+
+using namespace fame;
+
+extern "C" {
+
+int fame_autotune(fame_plan_t h, int prec, int nvec, int* chunk, int* stencil_tpb, double* us) {
+  if (!h) return FAME_ERR_BAD_ARG;
+  Plan& P = h->P;
+  if (nvec < 1 || (prec != FAME_C64 && prec != FAME_C128)) return fail(&P, FAME_ERR_BAD_ARG, "fame_autotune: bad argument");
+  TuneEntry b;
+  const int rc = prec == FAME_C64 ? autotune_prec<float>(P, nvec, 5, &b) : autotune_prec<double>(P, nvec, 5, &b);
+  if (rc != FAME_OK) return rc;
+  if (chunk) *chunk = b.chunk;
+  if (stencil_tpb) *stencil_tpb = b.stencil_tpb;
+  if (us) *us = b.us;
+  return FAME_OK;
+}
+
+int fame_set_tune(fame_plan_t h, int prec, int nvec, int chunk, int stencil_tpb) {
+  if (!h) return FAME_ERR_BAD_ARG;
+  Plan& P = h->P;
+  if (nvec < 1 || chunk < 0 || (stencil_tpb != 128 && stencil_tpb != 256 && stencil_tpb != 512) ||
+      (prec != FAME_C64 && prec != FAME_C128))
+    return fail(&P, FAME_ERR_BAD_ARG, "fame_set_tune: bad argument");
+  TuneEntry t;
+  t.prec = prec;
+  t.nvec = nvec;
+  t.chunk = chunk >= nvec ? 0 : chunk;
+  t.stencil_tpb = stencil_tpb;
+  put_tune(P, t);
+  return FAME_OK;
+}
+
+}  // extern "C"

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -19,12 +20,32 @@ extern unsigned long long g_kernel_launches;
 // Which vectors of a batch belong to which k-point instance, and which are
 // still active (converged vectors of a batched solve are skipped).
 struct VecCtx {
-  const int* inst = nullptr;    // device [nvec] instance index, or null: v % nk
+  const int* inst = nullptr;    // device [nvec] instance index, or null: (v + vofs) % nk
   const int* active = nullptr;  // device [nvec] 0/1, or null: all active
   int nk = 1;
+  int vofs = 0;                 // index of vector 0 in the caller's batch (sub-batches)
 };
 
-FAME_HD int vec_inst(const VecCtx& c, int v) { return c.inst ? c.inst[v] : (v % c.nk); }
+FAME_HD int vec_inst(const VecCtx& c, int v) { return c.inst ? c.inst[v] : ((v + c.vofs) % c.nk); }
+
+// The same context for the sub-batch of vectors [v0, ...).
+inline VecCtx sub_ctx(const VecCtx& c, int v0) {
+  VecCtx s = c;
+  if (s.inst) s.inst += v0;
+  if (s.active) s.active += v0;
+  s.vofs += v0;
+  return s;
+}
+
+// Launch parameters of the fncB sequence picked by fame_autotune for one
+// (precision, batch width): vectors per launch sequence and threads per block
+// of the stencil kernels.
+struct TuneEntry {
+  int prec = 0, nvec = 0;
+  int chunk = 0;         // 0: whole batch
+  int stencil_tpb = 256;
+  double us = 0.0;       // measured time of one fncB on the batch
+};
 
 // Device-side data of one precision.
 template <class R> struct PlanData {
@@ -94,7 +115,12 @@ struct Plan {
   // captured launch sequences (graph.cu)
   cudaStream_t cap_stream = nullptr;
   std::vector<GraphEntry> graphs;
+  // autotuned fncB launch parameters (autotune.cu)
+  std::vector<TuneEntry> tune;
 };
+
+// Tuned launch parameters for (prec, nvec), or the defaults.
+TuneEntry tune_for(const Plan& P, int prec, int nvec);
 
 // Replay the launch sequence that `issue(stream)` enqueues, from a graph cached
 // under `key` (captured on first use on a private stream), on the plan's

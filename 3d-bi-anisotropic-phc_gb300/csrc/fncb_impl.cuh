@@ -343,21 +343,34 @@ cudaError_t col(const PlanData<R>& d, cx<R>* w, int nfield, int nvec, long long 
 }
 
 
+// fncB on a batch, as sub-batches of `chunk` vectors (0: all at once) so that
+// the six-field intermediates of a sub-batch can stay in L2; the stencil
+// kernels run with tpb threads per block.  Both come from fame_autotune.
 template <class R, int N>
 cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx, cx<R>* w0, cx<R>* w1,
                    cudaStream_t st) {
   const PlanData<R>& d = pdata<R>(P);
   const long long Nq = P.Nq;
-  cudaError_t e;
-  e = plane_inv<R, N, true, false>(P, d, x, w0, nvec, 2, 0, 4 * Nq, 2 * Nq, 6 * Nq, ctx, st);
-  if (e != cudaSuccess) return e;
-  e = col<R, N, +1, 0>(d, w0, 6, nvec, 6 * Nq, ctx, st);
-  if (e != cudaSuccess) return e;
-  e = stencil_n<R, N>(P, w0, w1, nvec, ctx, st);
-  if (e != cudaSuccess) return e;
-  e = col<R, N, -1, 0>(d, w0, 6, nvec, 6 * Nq, ctx, st);
-  if (e != cudaSuccess) return e;
-  return plane_fwd<R, N, true, false>(P, d, w0, y, nvec, 2, 0, 6 * Nq, 4 * Nq, 2 * Nq, ctx, st);
+  const TuneEntry tn = tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec);
+  const int chunk = (tn.chunk > 0 && tn.chunk < nvec) ? tn.chunk : nvec;
+  for (int v0 = 0; v0 < nvec; v0 += chunk) {
+    const int nv = std::min(chunk, nvec - v0);
+    const VecCtx c = sub_ctx(ctx, v0);
+    const cx<R>* xs = x + (size_t)v0 * 4 * Nq;
+    cx<R>* ys = y + (size_t)v0 * 4 * Nq;
+    cudaError_t e;
+    e = plane_inv<R, N, true, false>(P, d, xs, w0, nv, 2, 0, 4 * Nq, 2 * Nq, 6 * Nq, c, st);
+    if (e != cudaSuccess) return e;
+    e = col<R, N, +1, 0>(d, w0, 6, nv, 6 * Nq, c, st);
+    if (e != cudaSuccess) return e;
+    e = stencil_n<R, N>(P, w0, w1, nv, c, st, tn.stencil_tpb);
+    if (e != cudaSuccess) return e;
+    e = col<R, N, -1, 0>(d, w0, 6, nv, 6 * Nq, c, st);
+    if (e != cudaSuccess) return e;
+    e = plane_fwd<R, N, true, false>(P, d, w0, ys, nv, 2, 0, 6 * Nq, 4 * Nq, 2 * Nq, c, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 template <class R, int N>
@@ -419,7 +432,8 @@ cudaError_t handle_n(const Plan& P, int which, const cx<R>* x, cx<R>* y, int nve
 #define FAME_SIZE_SIGS(PFX, R, NN)                                                                                 \
   PFX cudaError_t fame::detail::fncB_n<R, NN>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&, cx<R>*,       \
                                               cx<R>*, cudaStream_t);                                               \
-  PFX cudaError_t fame::detail::stencil_n<R, NN>(const Plan&, cx<R>*, cx<R>*, int, const VecCtx&, cudaStream_t);  \
+  PFX cudaError_t fame::detail::stencil_n<R, NN>(const Plan&, cx<R>*, cx<R>*, int, const VecCtx&, cudaStream_t,    \
+                                                 int);                                                             \
   PFX cudaError_t fame::detail::fields_inv_n<R, NN>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&,         \
                                                     cudaStream_t);                                                 \
   PFX cudaError_t fame::detail::transform_n<R, NN>(const Plan&, int, const cx<R>*, cx<R>*, int, const VecCtx&,     \

@@ -23,11 +23,11 @@ template <> inline const PlanData<double>& pdata<double>(const Plan& P) { return
 template <> inline const PlanData<float>& pdata<float>(const Plan& P) { return P.d32; }
 
 template <class R, int N>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 k_vertex(const cx<R>* __restrict__ uv, cx<R>* __restrict__ h, PlanData<R> d,
          const uint8_t* __restrict__ phase, int nphase, VecCtx ctx, long long stride) {
   constexpr int NN = N * N, Nq = NN * N;
-  const int idx = blockIdx.x * 256 + threadIdx.x;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   const int vec = blockIdx.y;
   if (idx >= Nq) return;
   if (ctx.active && !ctx.active[vec]) return;
@@ -95,11 +95,11 @@ k_vertex(const cx<R>* __restrict__ uv, cx<R>* __restrict__ h, PlanData<R> d,
 }
 
 template <class R, int N>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 k_faceedge(cx<R>* __restrict__ uv, const cx<R>* __restrict__ h, PlanData<R> d,
            const uint8_t* __restrict__ phase, int nphase, VecCtx ctx, long long stride) {
   constexpr int NN = N * N, Nq = NN * N;
-  const int idx = blockIdx.x * 256 + threadIdx.x;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   const int vec = blockIdx.y;
   if (idx >= Nq) return;
   if (ctx.active && !ctx.active[vec]) return;
@@ -157,17 +157,20 @@ k_faceedge(cx<R>* __restrict__ uv, const cx<R>* __restrict__ h, PlanData<R> d,
   for (int c = 0; c < 6; ++c) f[c * Nq] = r[c];
 }
 
-// In place on w (6-field vectors, stride 6*Nq), scratch h of the same size.
+// In place on w (6-field vectors, stride 6*Nq), scratch h of the same size;
+// tpb threads per block (128, 256 or 512).
 template <class R, int N>
-cudaError_t stencil_n(const Plan& P, cx<R>* w, cx<R>* h, int nvec, const VecCtx& ctx, cudaStream_t st) {
+cudaError_t stencil_n(const Plan& P, cx<R>* w, cx<R>* h, int nvec, const VecCtx& ctx, cudaStream_t st,
+                      int tpb = 256) {
   constexpr int Nq = N * N * N;
-  const dim3 g((Nq + 255) / 256, nvec);
+  if (tpb != 128 && tpb != 512) tpb = 256;
+  const dim3 g((Nq + tpb - 1) / tpb, nvec);
   FAME_LAUNCHED(1);
-  k_vertex<R, N><<<g, 256, 0, st>>>(w, h, pdata<R>(P), P.d_phase, P.nphase, ctx, 6LL * Nq);
+  k_vertex<R, N><<<g, tpb, 0, st>>>(w, h, pdata<R>(P), P.d_phase, P.nphase, ctx, 6LL * Nq);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   FAME_LAUNCHED(1);
-  k_faceedge<R, N><<<g, 256, 0, st>>>(w, h, pdata<R>(P), P.d_phase, P.nphase, ctx, 6LL * Nq);
+  k_faceedge<R, N><<<g, tpb, 0, st>>>(w, h, pdata<R>(P), P.d_phase, P.nphase, ctx, 6LL * Nq);
   return cudaGetLastError();
 }
 

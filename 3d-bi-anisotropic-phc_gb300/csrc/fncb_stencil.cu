@@ -64,7 +64,7 @@ namespace detail {
 template <class R>
 cudaError_t stencil(const Plan& P, cx<R>* w, cx<R>* h, int nvec, const VecCtx& ctx, cudaStream_t st) {
   switch (P.n) {
-#define FAME_CASE(NN) case NN: return stencil_n<R, NN>(P, w, h, nvec, ctx, st);
+#define FAME_CASE(NN) case NN: return stencil_n<R, NN>(P, w, h, nvec, ctx, st, 256);
     FAME_FOR_EACH_N(FAME_CASE)
 #undef FAME_CASE
     default: return cudaErrorInvalidValue;

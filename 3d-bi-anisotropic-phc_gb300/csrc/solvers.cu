@@ -156,7 +156,9 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
                                        (uintptr_t)p, (uintptr_t)q, (uintptr_t)x, (uintptr_t)r, (uintptr_t)z,
                                        (uintptr_t)w0, (uintptr_t)w1, (uintptr_t)s, (uintptr_t)part,
                                        (uintptr_t)d_inst, (uintptr_t)nblk, (uintptr_t)nblkv,
-                                       sizeof(R) == 4 ? (uintptr_t)P.d32.pc : (uintptr_t)P.d64.pc};
+                                       sizeof(R) == 4 ? (uintptr_t)P.d32.pc : (uintptr_t)P.d64.pc,
+                                       (uintptr_t)tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).chunk,
+                                       (uintptr_t)tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).stencil_tpb};
   bool use_graph = P.opt_graph != 0;
   bool any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
   for (int it = 1; it <= maxit && any; it += chk) {

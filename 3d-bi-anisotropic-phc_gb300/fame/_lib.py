@@ -66,6 +66,8 @@ SIGNATURES = {
     "fame_set_field": (_i, [_vp, _pd, _pd]),
     "fame_eig_gradient": (_i, [_vp, _i, _pi, _vp, _pd, _pd, _vp, _vp, _i, _pd]),
     "fame_restore": (_i, [_vp, _i, _pi, _vp, _pd, _vp, _vp, _pd, _pd, _pd, _i]),
+    "fame_autotune": (_i, [_vp, _i, _i, _pi, _pi, _pd]),
+    "fame_set_tune": (_i, [_vp, _i, _i, _i, _i]),
 }
 
 

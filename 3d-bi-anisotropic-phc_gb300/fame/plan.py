@@ -212,6 +212,40 @@ class Plan:
         check(self._lib.fame_set_option(self._h, int(code), float(value)), self._h, "fame_set_option")
         return self
 
+    def autotune(self, nvec=None, prec="c64", cache=None):
+        """fame_autotune for batch width `nvec` (default: the plan's instance
+        count).  With `cache` (a JSON file path) a setting measured before on
+        the same device, grid, precision and width is installed without
+        re-timing, and new measurements are added to the file.
+        Returns dict(chunk, stencil_tpb, us, cached)."""
+        import json
+        import os
+        nvec = self.nk if nvec is None else int(nvec)
+        pr = L.FAME_C64 if prec in ("c64", L.FAME_C64) else L.FAME_C128
+        dev = torch.cuda.get_device_name() if torch is not None and torch.cuda.is_available() else "gpu"
+        key = f"{dev}|n={self.n}|{'c64' if pr == L.FAME_C64 else 'c128'}|nvec={nvec}"
+        table = {}
+        if cache and os.path.exists(cache):
+            with open(cache) as f:
+                table = json.load(f)
+        if key in table:
+            t = table[key]
+            check(self._lib.fame_set_tune(self._h, pr, nvec, int(t["chunk"]), int(t["stencil_tpb"])), self._h,
+                  "fame_set_tune")
+            return dict(t, cached=True)
+        ch, tpb, us = C.c_int(), C.c_int(), C.c_double()
+        self._stream()
+        check(self._lib.fame_autotune(self._h, pr, nvec, C.byref(ch), C.byref(tpb), C.byref(us)), self._h,
+              "fame_autotune")
+        t = dict(chunk=ch.value, stencil_tpb=tpb.value, us=us.value)
+        if cache:
+            table[key] = t
+            tmp = cache + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(table, f, indent=1, sort_keys=True)
+            os.replace(tmp, cache)
+        return dict(t, cached=False)
+
     # -- generic call -------------------------------------------------------
     def _call(self, fn, x, out_len, inst, *extra, name=""):
         prec = _prec_of(x)

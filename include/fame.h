@@ -84,6 +84,18 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *                     on first use [1]; 0 launches every kernel directly. */
 enum fame_option { FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2 };
 int fame_set_option(fame_plan_t plan, int option, double value);
+
+/*
+ * Autotuner (no reference counterpart): time the launch parameters of the
+ * fncB sequence for precision `prec` and batch width `nvec` on this plan
+ * (vectors per launch sequence: the whole batch or 1/2, 1/4, 1/8 of it;
+ * threads per block of the stencil kernels: 128, 256, 512) and keep the
+ * fastest for later calls with that width.  Outputs (may be NULL): the chosen
+ * chunk (0 = whole batch), block size and the measured microseconds of one
+ * fncB.  fame_set_tune installs a setting directly (e.g. from a cache).
+ */
+int fame_autotune(fame_plan_t plan, int prec, int nvec, int* chunk, int* stencil_tpb, double* us);
+int fame_set_tune(fame_plan_t plan, int prec, int nvec, int chunk, int stencil_tpb);
 int fame_sync(fame_plan_t plan);
 const char* fame_last_error(fame_plan_t plan);
 int fame_plan_info(fame_plan_t plan, int* n, int* nk, long long* nq);

@@ -1,0 +1,43 @@
+"""Uneven-grid batch (fame.batch): plans of several grid sizes solved
+concurrently on their own streams give the same eigenvalues as solving each
+instance alone, and the autotuner's choice leaves fncB unchanged."""
+import numpy as np
+import pytest
+import torch
+
+import fame
+import fame.batch as FB
+
+pytestmark = pytest.mark.gpu
+
+
+def test_uneven_concurrent_matches_single_instances(cuda, fame_lib):
+    groups = FB.uneven_workload(seed=3, sizes=(8, 12), per_size=3, bands=(3, 5))
+    res, wall = FB.solve_uneven(groups, prec="c128", tol=1e-10, concurrent=True)
+    seq, _ = FB.solve_uneven(groups, prec="c128", tol=1e-10, concurrent=False, autotune=False)
+    for g, r, s in zip(groups, res, seq):
+        assert r["status"] == 0 and s["status"] == 0
+        for i in range(len(g["kvecs"])):
+            assert len(r["omega"][i]) == g["bands"][i]
+            assert np.allclose(r["omega"][i], s["omega"][i], rtol=1e-10)
+        # instance 0 on its own plan
+        plan = fame.woodpile_plan(g["n"], g["kvecs"][:1], gamma=float(g["gammas"][0]))
+        k = int(g["bands"][0])
+        one = plan.lanczos(k, tol=1e-10, prec="c128", p=max(2 * k, 20), want_vectors=False)
+        assert np.allclose(np.sort(one["omega"]), r["omega"][0], rtol=1e-9)
+
+
+@pytest.mark.parametrize("dtype", ["c64", "c128"])
+def test_autotuned_fncB_unchanged(cuda, fame_lib, dtype):
+    plan = fame.woodpile_plan(12, fame.band_path(npts=40)[:5])
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((5, 4 * 12 ** 3)) + 1j * rng.standard_normal((5, 4 * 12 ** 3))
+    xt = torch.as_tensor(x).to(torch.complex64 if dtype == "c64" else torch.complex128).cuda()
+    y0 = plan.apply_B(xt)
+    t = plan.autotune(nvec=5, prec=dtype)
+    assert t["chunk"] in (0, 1, 2, 3) and t["stencil_tpb"] in (128, 256, 512) and t["us"] > 0
+    for chunk in (1, 2, 0):
+        for tpb in (128, 512):
+            fame.load().fame_set_tune(plan.raw, 1 if dtype == "c64" else 0, 5, chunk, tpb)
+            y = plan.apply_B(xt)
+            assert torch.equal(y, y0), (chunk, tpb)

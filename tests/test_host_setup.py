@@ -81,3 +81,14 @@ def test_tetra_inside_matches_oracle_isofun():
     got = fame.tetra_inside(P, edge, A)
     assert got.sum() > 0
     assert np.array_equal(got, ref)
+
+
+def test_ibz_points_in_wedge():
+    import fame.batch as FB
+    k = FB.ibz_kpoints(200, seed=1) / (2 * np.pi)
+    assert np.all(k[:, 2] <= k[:, 0] + 1e-15) and np.all(k[:, 0] <= k[:, 1] + 1e-15)
+    assert np.all(k.sum(axis=1) <= 1.5 + 1e-12) and np.all(k <= 1.0)
+    # the high-symmetry points bounding the wedge, in fame.fcc_point's orientation
+    for lab in "GXLWKU":
+        q = fame.fcc_point(lab) / (2 * np.pi)
+        assert q[2] <= q[0] + 1e-12 <= q[1] + 2e-12 and q.sum() <= 1.5 + 1e-12
