@@ -8,7 +8,7 @@ MATLAB handles (``fncA``, ``fncB``, ``fncinvB``, ``MtxVecMul_FFT``,
 """
 from ._lib import FameError, lib_path, load  # noqa: F401
 from . import adjoint  # noqa: F401
-from .handles import Lanczos, MtxVecMul_FFT, fncA, fncB, fncinvB, woodpile_plan  # noqa: F401
+from .handles import Lanczos, Lanczos_gep, MtxVecMul_FFT, fncA, fncB, fncinvB, woodpile_plan  # noqa: F401
 from .plan import Plan  # noqa: F401
 from .setup import (band_path, bi_isotropic, bloch_angles, constitutive, covariant_blocks,  # noqa: F401
                     fcc_lattice, fcc_point, reference_path, sphere_inside, tetra_inside, vertex_positions,

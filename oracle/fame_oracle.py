@@ -31,7 +31,7 @@ __all__ = [
     "fncinvB", "lanczos", "eigen_restoration", "evaluate_error",
     "BandProblem", "build_problem", "woodpile_phases", "fft_workers",
     "field_diagonals", "build_problem_field", "material_quad_coeffs", "field_gradient",
-    "chiral_noise_field",
+    "chiral_noise_field", "lanczos_gep", "gsreorthog",
 ]
 
 _W = max(1, min(8, os.cpu_count() or 1))
@@ -847,3 +847,111 @@ def chiral_noise_field(n, seed=0, sigma=2.0, slope=8.0, eps_lo=1.0, eps_span=12.
     s = 1.0 / (1.0 + np.exp(-slope * sm))
     s = s.reshape(-1)
     return eps_lo + eps_span * s, gamma_max * s
+
+
+# --------------------------------------------------------------------------
+# Implicitly restarted Lanczos (subroutines/Lanczos_gep.m)
+# --------------------------------------------------------------------------
+def gsreorthog(Q, fB, x):
+    """``subroutines/Lanczos_gep.m:103-142``: B-orthogonalise ``x`` against
+    the columns of ``Q`` by classical Gram-Schmidt repeated while the squared
+    B-norm drops below half (Kahan-Parlett), with the reference's fallback to
+    a unit vector.  Returns ``(p, r, tho)`` with ``x = Q r + tho p``."""
+    n = Q.shape[1]
+    r = np.zeros(n, dtype=np.complex128)
+    tho = np.vdot(x, fB(x)).real
+    if tho == 0:
+        return np.zeros_like(x), r, 0.0
+    mu = tho
+    x_bar = x.copy()
+    nrm = [np.vdot(Q[:, i], fB(Q[:, i])).real for i in range(n)]
+    k = int(np.argmin(nrm))          # first index of the minimal B-norm (:117-125)
+    ei = np.zeros(x.shape[0], dtype=np.complex128)
+    ei[k] = 1.0
+    eps = np.finfo(float).eps
+    while True:
+        s = Q.conj().T @ fB(x_bar)
+        r = r + s
+        x_bar = x_bar - Q @ s
+        tau = np.vdot(x_bar, fB(x_bar)).real
+        if tau / tho >= 0.5:
+            break
+        if tau > 0.1 * mu * eps:
+            tho = tau
+        else:
+            tho = 0.1 * tho * eps
+            mu = tho
+            x_bar = ei.copy()
+    tho = math.sqrt(np.vdot(x_bar, fB(x_bar)).real)
+    return x_bar / tho, r, tho
+
+
+def _implicit_restart(Q, alpha, beta, k, m, fB=None):
+    """``Lanczos_gep.m:45-82``: m-k exact shifts at the Ritz values of smallest
+    magnitude, band-truncated symmetrised QR steps, new length-k decomposition.
+    The new residual vector is scaled by its Euclidean norm as ``:77`` does
+    (``rho = norm(P)``); with ``fB`` given, by its B-norm instead, which keeps
+    the basis B-orthonormal."""
+    T = np.diag(alpha[:m]) + np.diag(beta[:m - 1], -1) + np.diag(beta[:m - 1], 1)
+    ritz = np.linalg.eigvalsh(T)
+    unwanted = ritz[np.argsort(np.abs(ritz), kind="stable")[:m - k]]
+    e = np.zeros(m)
+    e[m - 1] = 1.0
+    I = np.eye(m)
+    U_total = I.copy()
+    for mu in unwanted:
+        U, R = np.linalg.qr(T - mu * I)
+        U_total = U_total @ U
+        T = R @ U + mu * I
+        for j in range(m - 2):
+            T[j, j + 2:] = 0.0
+        T = (T + T.T) / 2
+    b = U_total.T @ e
+    Qm = Q[:, :m] @ U_total
+    P = T[k, k - 1] * Qm[:, k] + beta[m - 1] * b[k - 1] * Q[:, m]
+    rho = np.linalg.norm(P) if fB is None else math.sqrt(np.vdot(P, fB(P)).real)
+    Qn = np.zeros_like(Q)
+    Qn[:, :k] = Qm[:, :k]
+    Qn[:, k] = P / rho
+    alpha = alpha.copy()
+    beta = beta.copy()
+    beta[:k] = np.concatenate([np.diag(T, -1)[:k - 1], [rho]])
+    alpha[:k] = np.diag(T)[:k]
+    return Qn, alpha, beta
+
+
+def lanczos_gep(fA, fB, fBinv, n, k, m, itmax, tol, v0, bnorm_restart=False):
+    """``subroutines/Lanczos_gep.m:1-27`` line by line: start vector
+    ``v0/(v0' B v0)``, Lanczos steps ``alpha_j = Re(q_j' A q_j)``,
+    ``r = B^{-1} A q_j - alpha_j q_j - beta_{j-1} q_{j-1}`` B-orthogonalised
+    by ``gsreorthog``, implicit restarts, stop when ``|beta_k| < tol |alpha_k|``.
+    Returns ``(EV, EW, nit)`` with EW ascending (eig of the k x k tridiagonal).
+    ``bnorm_restart`` replaces the Euclidean scaling of the restart vector
+    (``:77``) by the B-norm (see ``_implicit_restart``)."""
+    Q = np.zeros((n, m + 1), dtype=np.complex128)
+    v0 = np.asarray(v0, dtype=np.complex128)
+    Q[:, 0] = v0 / np.vdot(v0, fB(v0)).real
+    alpha = np.zeros(m)
+    beta = np.zeros(m)
+
+    def steps(Q, alpha, beta, k0):
+        for j in range(k0, m):
+            temp = fA(Q[:, j])
+            alpha[j] = np.vdot(Q[:, j], temp).real
+            r = fBinv(temp) - alpha[j] * Q[:, j]
+            if j > 0:
+                r = r - beta[j - 1] * Q[:, j - 1]
+            Q[:, j + 1], _, beta[j] = gsreorthog(Q[:, :j + 1], fB, r)
+        return Q, alpha, beta
+
+    Q, alpha, beta = steps(Q, alpha, beta, 0)
+    nit = 0
+    while nit < itmax:
+        nit += 1
+        Q, alpha, beta = steps(Q, alpha, beta, k)
+        Q, alpha, beta = _implicit_restart(Q, alpha, beta, k, m, fB if bnorm_restart else None)
+        if abs(beta[k - 1]) < tol * abs(alpha[k - 1]):
+            T = np.diag(alpha[:k]) + np.diag(beta[:k - 1], -1) + np.diag(beta[:k - 1], 1)
+            ew, V = np.linalg.eigh(T)
+            return Q[:, :k] @ V, ew, nit
+    return None, None, nit
