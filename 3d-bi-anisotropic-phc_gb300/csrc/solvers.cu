@@ -518,7 +518,11 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         }
     }
     prof.mark(1);
-    // orthogonalisation (Lanczos.m:53-69)
+    // orthogonalisation (Lanczos.m:53-69); the full Gram-Schmidt of :69 as
+    // classical GS with a second pass when the first cancelled much of r
+    // (||c||^2 > ||r||_B^2 / 2, the DGKS test).  The mixed form carries B r,
+    // which gives ||r||_B; the FP64 form always takes the second pass.
+    std::vector<int> second(na, 0);
     for (int a = 0; a < na; ++a) {
       if (S[a].done) continue;
       LzInst& I = S[a];
@@ -537,10 +541,29 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         if ((rc = project_out(a, r, br, j - 1, 1))) return rc;  // :63
       }
       if ((rc = project_out(a, r, br, j, 1))) return rc;  // :66
-      if ((rc = project_out(a, r, br, 0, I.j))) return rc;  // :69 (two passes)
-      if ((rc = project_out(a, r, br, 0, I.j))) return rc;
+      if (mixed)  // ||r||_B^2 before the full pass, next to the pass's coefficients
+        FAME_CK(dot_batched<double>(r, 0, L, 1, br, 0, L, 1, coef + (size_t)a * 128 + 127, part, nblk1, nullptr, st),
+                "lanczos norm");
+      if ((rc = project_out(a, r, br, 0, I.j))) return rc;  // :69, first pass
+      second[a] = 1;
       I.steps++;
     }
+    if (mixed) {
+      std::vector<double2> hc((size_t)na * 128);
+      FAME_CK(cudaMemcpyAsync(hc.data(), coef, sizeof(double2) * hc.size(), cudaMemcpyDeviceToHost, st), "lanczos gs");
+      FAME_CK(cudaStreamSynchronize(st), "lanczos gs");
+      for (int a = 0; a < na; ++a) {
+        if (!second[a]) continue;
+        double c2 = 0.0;
+        for (int i = 0; i < S[a].j; ++i) c2 += hc[(size_t)a * 128 + i].x * hc[(size_t)a * 128 + i].x +
+                                               hc[(size_t)a * 128 + i].y * hc[(size_t)a * 128 + i].y;
+        const double r2 = hc[(size_t)a * 128 + 127].x;
+        second[a] = !(c2 <= 0.5 * r2);
+      }
+    }
+    for (int a = 0; a < na; ++a)
+      if (second[a] && !S[a].done)
+        if ((rc = project_out(a, PR + (size_t)a * L, mixed ? BPR + (size_t)a * L : nullptr, 0, S[a].j))) return rc;
     prof.mark(2);
     // rr = fncB(r); beta = sqrt(r'*rr); v = r/beta  (Lanczos.m:72-74)
     if (!mixed) {

@@ -41,8 +41,11 @@ N_GRID = 60
 BANDS = 10
 LANCZOS_TOL = 1e-10
 INNER_TOL = 1e-12          # B^{-1} of the plain FP64 form (the reference's pcg tolerance)
-INNER_TOL_MIXED = 1e-12    # B^{-1} of the mixed form (complex64 CG + FP64 residual refinement;
-                           # tightened per k-point by the Ritz-value spread, see solvers.cu)
+INNER_TOL_MIXED = 1e-11    # B^{-1} of the mixed form (complex64 CG + FP64 residual refinement;
+                           # tightened per k-point by the Ritz-value spread, see solvers.cu).
+                           # Two complex64 rounds reach it with one FP64 residual; 1e-12 needs a
+                           # third round.  Measured at n = 60: residuals <= 2e-9 (bar 1e-8),
+                           # eigenvalues within 5e-10 of the FP64 form (reported per run).
 RES_TOL = 1e-8
 PATH_POINTS = 40
 # B applies (fncB) of one plain-FP64 Lanczos band solve at n = 60 on this path
