@@ -294,7 +294,7 @@ def run_fame(args):
                                    "40-point path G-X-U|K-G-L-W-X, 10 bands, Lanczos tol 1e-10, res<=1e-8",
                        "n": N_GRID, "bands": BANDS, "kpoints_per_step": args.batch, "path_kpoints": PATH_POINTS,
                        "precision": "complex64 fncB + preconditioned CG, FP64 recurrence/reorth/residual "
-                                    "refinement (B^-1 to 1e-12, tighter near Gamma)/NFSEP check",
+                                    f"refinement (B^-1 to {INNER_TOL_MIXED:g}, tighter near Gamma)/NFSEP check",
                        "l2": "inputs larger than L2 (Lanczos basis and B*Q of a batch ~4.4 GB)"},
             "e2e": {"value": None if e2e_value is None else round(e2e_value, 5), "unit": UNIT,
                     "h2d_bytes_per_step": int(h2d / max(1, e2e_steps)),
@@ -394,7 +394,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=8, help="k-points per step (batched band solve)")
     ap.add_argument("--impl", choices=["fame", "reference"], default="fame")
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=5,
+                    help="end-to-end steps (capped at --steps; the same batches as the timed steps)")
     ap.add_argument("--fp64-kpoints", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-applies", type=int, default=10)
