@@ -143,6 +143,8 @@ def run_fame(args):
 
     import fame
 
+    from fame.shard import batch_index, max_over_ranks, whole_job_rate
+
     rank, world, local = env_rank()
     torch.cuda.set_device(local)
     if world > 1:
@@ -150,7 +152,7 @@ def run_fame(args):
     lib = fame.load()
     path, batches = path_batches(args.batch)
     nb = len(batches)
-    bidx = lambda s: (s * world + rank) % nb
+    bidx = lambda s: batch_index(s, rank, world, nb)
     needed = sorted({bidx(s) for s in range(args.warmup + args.steps)})
     plans = {b: fame.woodpile_plan(N_GRID, batches[b]) for b in needed}
 
@@ -179,13 +181,8 @@ def run_fame(args):
     if world > 1:
         dist.barrier()
     t = e0.elapsed_time(e1) / 1000.0
-    tmax = t
-    if world > 1:
-        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        tmax = float(tt.item())
-    nk_total = args.steps * args.batch * world
-    value = nk_total / tmax
+    tmax = max_over_ranks(t, device="cuda")
+    value = whole_job_rate(args.batch, args.steps, world, tmax)
     res_max = max(float(np.max(r["res"])) for r in results)
     worst = None
     for s, r in enumerate(results):
@@ -219,12 +216,8 @@ def run_fame(args):
         h2d += phase_host.nbytes + th.nbytes + tens.nbytes * len(kv)
         d2h += r["ew"].nbytes + r["res"].nbytes + r["stats"].nbytes
     torch.cuda.synchronize()
-    te = time.perf_counter() - t0
-    if world > 1:
-        tt = torch.tensor([te], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        te = float(tt.item())
-    e2e_value = e2e_steps * args.batch * world / te if e2e_steps else None
+    te = max_over_ranks(time.perf_counter() - t0, device="cuda")
+    e2e_value = whole_job_rate(args.batch, e2e_steps, world, te) if e2e_steps else None
 
     out = None
     if rank == 0:
