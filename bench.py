@@ -380,6 +380,26 @@ def profile_fncb(nvec, prec):
     plan.close()
 
 
+def profile_cg(nvec):
+    """Two preconditioned complex64 CG solves of 4 iterations on `nvec` vectors
+    at n=60 (first `nvec` path k-points after Gamma), every kernel launched
+    directly (graph replay off): the workload of the committed CG launch list."""
+    import torch
+
+    import fame
+
+    torch.cuda.set_device(0)
+    path = fame.band_path(npts=PATH_POINTS)
+    plan = fame.woodpile_plan(N_GRID, path[8 + np.arange(nvec) % (len(path) - 8)])
+    plan.set_option("graph", 0)
+    x = torch.randn(nvec, 4 * N_GRID ** 3, dtype=torch.complex64, device="cuda")
+    for _ in range(2):
+        plan.apply_Binv(x, tol=1e-30, maxit=4)
+    torch.cuda.synchronize()
+    print(f"CG c64 n={N_GRID} x{nvec}: ok")
+    plan.close()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -395,9 +415,14 @@ def main():
     ap.add_argument("--profile-fncb", type=int, default=0, metavar="NVEC",
                     help="only apply fncB three times to NVEC vectors (for ncu captures) and exit")
     ap.add_argument("--profile-prec", choices=["c64", "c128"], default="c64")
+    ap.add_argument("--profile-cg", type=int, default=0, metavar="NVEC",
+                    help="only run two 4-iteration complex64 CG solves on NVEC vectors (for ncu) and exit")
     args = ap.parse_args()
     if args.profile_fncb > 0:
         profile_fncb(args.profile_fncb, args.profile_prec)
+        return
+    if args.profile_cg > 0:
+        profile_cg(args.profile_cg)
         return
     if args.impl == "reference":
         run_reference(args)
