@@ -53,7 +53,7 @@ template <class R> struct PlanData {
   cx<R>* tau = nullptr;  // [nk][3]   exp(i*theta_d/n): Bloch phase of one periodic shift
   cx<R>* sxyz = nullptr; // [nk][3n]  S_sDFT per axis (the MtxVecMul_FFT phase)
   cx<R>* mat = nullptr;  // [nk][nphase][27]: Herm(N) | Herm(M) | J, row-major 3x3 each
-  cx<R>* pc = nullptr;   // [nk][10][Nq] CG preconditioner: inverse 4x4 Hermitian blocks (lazy)
+  cx<R>* pc = nullptr;   // [nk][8][Nq] CG preconditioner: inverse 4x4 Hermitian blocks, diagonal packed (lazy)
   // Field mode (per-vertex isotropic chiral medium eps(r) I, mu = I,
   // xi = -zeta = i gamma(r) I): vertex tensors N = a G, M = b G, J = -i g G with
   // a = 1/(eps - gamma^2), b = eps a, g = gamma a and G = A^T A the lattice

@@ -20,6 +20,10 @@ namespace {
 
 __device__ __forceinline__ double2 dmk(double a, double b) { return make_double2(a, b); }
 
+// Complex slots per voxel of the stored inverse blocks (the four real
+// diagonal entries packed in two).
+constexpr int kPcSlots = 8;
+
 __global__ void __launch_bounds__(128)
 k_precond_build64(const double2* __restrict__ lam_all, const double2* __restrict__ avg_all, int n, double2* pc64,
                   float2* pc32) {
@@ -107,23 +111,35 @@ k_precond_build64(const double2* __restrict__ lam_all, const double2* __restrict
   if (!ok)  // not positive definite (non-physical material): identity
     for (int a = 0; a < 4; ++a)
       for (int b = 0; b < 4; ++b) Minv[a][b] = dmk(a == b ? 1.0 : 0.0, 0.0);
-  const int ent[10][2] = {{0, 0}, {1, 1}, {2, 2}, {3, 3}, {0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
-  for (int e = 0; e < 10; ++e) {
-    double2 v = Minv[ent[e][0]][ent[e][1]];
-    if (e < 4) v.y = 0.0;
-    const long long o = ((long long)inst * 10 + e) * Nq + idx;
-    if (pc64) pc64[o] = v;
-    if (pc32) pc32[o] = make_float2(float(v.x), float(v.y));
+  // packed: (m00, m11) | (m22, m33) | m01 | m02 | m03 | m12 | m13 | m23
+  double2 v[kPcSlots];
+  v[0] = dmk(Minv[0][0].x, Minv[1][1].x);
+  v[1] = dmk(Minv[2][2].x, Minv[3][3].x);
+  const int ent[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+  for (int e = 0; e < 6; ++e) v[2 + e] = Minv[ent[e][0]][ent[e][1]];
+  for (int e = 0; e < kPcSlots; ++e) {
+    const long long o = ((long long)inst * kPcSlots + e) * Nq + idx;
+    if (pc64) pc64[o] = v[e];
+    if (pc32) pc32[o] = make_float2(float(v[e].x), float(v[e].y));
   }
 }
 
+// The inverse block of one voxel.
+template <class R> struct Block4 {
+  cx<R> s[kPcSlots];
+};
+template <class R>
+__device__ __forceinline__ Block4<R> load_block(const cx<R>* __restrict__ pc, long long Nq, long long idx) {
+  Block4<R> b;
+#pragma unroll
+  for (int e = 0; e < kPcSlots; ++e) b.s[e] = pc[e * Nq + idx];
+  return b;
+}
 // z = M r for the 4 components of one voxel
 template <class R>
-__device__ __forceinline__ void mvec4(const cx<R>* __restrict__ pc, long long Nq, long long idx, const cx<R> r[4],
-                                      cx<R> z[4]) {
-  const R m00 = pc[0 * Nq + idx].x, m11 = pc[1 * Nq + idx].x, m22 = pc[2 * Nq + idx].x, m33 = pc[3 * Nq + idx].x;
-  const cx<R> m01 = pc[4 * Nq + idx], m02 = pc[5 * Nq + idx], m03 = pc[6 * Nq + idx];
-  const cx<R> m12 = pc[7 * Nq + idx], m13 = pc[8 * Nq + idx], m23 = pc[9 * Nq + idx];
+__device__ __forceinline__ void mvec4(const Block4<R>& b, const cx<R> r[4], cx<R> z[4]) {
+  const R m00 = b.s[0].x, m11 = b.s[0].y, m22 = b.s[1].x, m33 = b.s[1].y;
+  const cx<R> m01 = b.s[2], m02 = b.s[3], m03 = b.s[4], m12 = b.s[5], m13 = b.s[6], m23 = b.s[7];
   z[0] = cfma(m03, r[3], cfma(m02, r[2], cfma(m01, r[1], cscale(r[0], m00))));
   z[1] = cfma(m13, r[3], cfma(m12, r[2], cfmac(m01, r[0], cscale(r[1], m11))));
   z[2] = cfma(m23, r[3], cfmac(m12, r[1], cfmac(m02, r[0], cscale(r[2], m22))));
@@ -164,14 +180,14 @@ k_precond_apply(const cx<R>* __restrict__ r, cx<R>* __restrict__ z, const cx<R>*
     if (threadIdx.x == 0) *out = make_double2(0.0, 0.0);
     return;
   }
-  const cx<R>* pc = pc_all + (long long)vec_inst(ctx, vec) * 10 * Nq;
+  const cx<R>* pc = pc_all + (long long)vec_inst(ctx, vec) * kPcSlots * Nq;
   const long long o = vec * 4 * Nq;
   R srz = 0, srr = 0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < Nq; i += (long long)nblk * blockDim.x) {
     cx<R> rv[4], zv[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) rv[c] = r[o + c * Nq + i];
-    mvec4<R>(pc, Nq, i, rv, zv);
+    mvec4<R>(load_block<R>(pc, Nq, i), rv, zv);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       z[o + c * Nq + i] = zv[c];
@@ -184,7 +200,7 @@ k_precond_apply(const cx<R>* __restrict__ r, cx<R>* __restrict__ z, const cx<R>*
 }
 
 template <class R>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 2 : 1)
 k_pcg_update(cx<R>* __restrict__ x, cx<R>* __restrict__ r, cx<R>* __restrict__ z, const cx<R>* __restrict__ p,
              const cx<R>* __restrict__ q, const cx<R>* __restrict__ pc_all, VecCtx ctx, long long Nq,
              const double* __restrict__ alpha, double2* __restrict__ partial) {
@@ -196,29 +212,52 @@ k_pcg_update(cx<R>* __restrict__ x, cx<R>* __restrict__ r, cx<R>* __restrict__ z
     return;
   }
   const R a = R(alpha[vec]);
-  const cx<R>* pc = pc_all + (long long)vec_inst(ctx, vec) * 10 * Nq;
+  const cx<R>* pc = pc_all + (long long)vec_inst(ctx, vec) * kPcSlots * Nq;
   const long long o = vec * 4 * Nq;
   R srz = 0, srr = 0;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < Nq; i += (long long)nblk * blockDim.x) {
-    cx<R> rv[4], zv[4];
+  const long long stride = (long long)nblk * blockDim.x;
+  // two voxels per pass, every load of both issued before any store
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < Nq; i += 2 * stride) {
+    const long long i2 = i + stride;
+    const bool two = i2 < Nq;
+    cx<R> pk[2][4], qk[2][4], xk[2][4], rk[2][4];
+    Block4<R> bk[2];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const long long k = o + c * Nq + i;
-      cx<R> pk = p[k], qk = q[k], xk = x[k], rk = r[k];
-      xk.x += a * pk.x;
-      xk.y += a * pk.y;
-      rk.x -= a * qk.x;
-      rk.y -= a * qk.y;
-      x[k] = xk;
-      r[k] = rk;
-      rv[c] = rk;
+    for (int u = 0; u < 2; ++u) {
+      if (u == 1 && !two) break;
+      const long long iv = u ? i2 : i;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const long long k = o + c * Nq + iv;
+        pk[u][c] = p[k];
+        qk[u][c] = q[k];
+        xk[u][c] = x[k];
+        rk[u][c] = r[k];
+      }
+      bk[u] = load_block<R>(pc, Nq, iv);
     }
-    mvec4<R>(pc, Nq, i, rv, zv);
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      z[o + c * Nq + i] = zv[c];
-      srz += rv[c].x * zv[c].x + rv[c].y * zv[c].y;
-      srr += rv[c].x * rv[c].x + rv[c].y * rv[c].y;
+    for (int u = 0; u < 2; ++u) {
+      if (u == 1 && !two) break;
+      const long long iv = u ? i2 : i;
+      cx<R> zv[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        xk[u][c].x += a * pk[u][c].x;
+        xk[u][c].y += a * pk[u][c].y;
+        rk[u][c].x -= a * qk[u][c].x;
+        rk[u][c].y -= a * qk[u][c].y;
+      }
+      mvec4<R>(bk[u], rk[u], zv);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const long long k = o + c * Nq + iv;
+        x[k] = xk[u][c];
+        r[k] = rk[u][c];
+        z[k] = zv[c];
+        srz += rk[u][c].x * zv[c].x + rk[u][c].y * zv[c].y;
+        srr += rk[u][c].x * rk[u][c].x + rk[u][c].y * rk[u][c].y;
+      }
     }
   }
   double2 s = block_sum2b(make_double2(double(srz), double(srr)));
@@ -241,7 +280,7 @@ template <class R> cudaError_t build_precond(Plan& P, cudaStream_t st) {
     e = cudaMemcpy(P.d_mat_avg, P.mat_avg.data(), sizeof(double2) * 27 * P.nk, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return e;
   }
-  e = cudaMalloc(&d.pc, sizeof(cx<R>) * 10 * (size_t)P.Nq * P.nk);
+  e = cudaMalloc(&d.pc, sizeof(cx<R>) * kPcSlots * (size_t)P.Nq * P.nk);
   if (e != cudaSuccess) return e;
   FAME_LAUNCHED(1);
   k_precond_build64<<<dim3((unsigned)((P.Nq + 127) / 128), P.nk), 128, 0, st>>>(
