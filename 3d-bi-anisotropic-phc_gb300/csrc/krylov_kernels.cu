@@ -159,8 +159,15 @@ __global__ void k_cg_p(cx<R>* __restrict__ p, const cx<R>* __restrict__ r, long 
   if (active && !active[vec]) return;
   const R b = R(beta[vec]);
   const long long o = vec * stride;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
-    cx<R> pi = p[o + i], ri = r[o + i];
+  const long long step = (long long)gridDim.x * blockDim.x;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + step < len; i += 2 * step) {  // both elements' loads before the stores
+    const cx<R> pi = p[o + i], ri = r[o + i], pj = p[o + i + step], rj = r[o + i + step];
+    p[o + i] = mk<R>(ri.x + b * pi.x, ri.y + b * pi.y);
+    p[o + i + step] = mk<R>(rj.x + b * pj.x, rj.y + b * pj.y);
+  }
+  if (i < len) {
+    const cx<R> pi = p[o + i], ri = r[o + i];
     p[o + i] = mk<R>(ri.x + b * pi.x, ri.y + b * pi.y);
   }
 }
