@@ -25,10 +25,12 @@
 // theta = 1/mu.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <complex>
 #include <numeric>
 #include <vector>
 
+#include "graph_impl.h"
 #include "krylov.h"
 #include "linalg_host.h"
 
@@ -50,8 +52,107 @@ enum JdWs { JD_V = 300, JD_BV, JD_AV, JD_VEC, JD_SMALL, JD_TMP, JD_PART, JD_R32,
 
 // MINRES (Paige & Saunders, 1975) on the Hermitian operator B - shift*A for one
 // vector: the Lanczos recurrence with Givens rotations, vectors in the
-// precision R, scalars in FP64, one host round trip per iteration.  The
-// reference's SIRA inner solver is MATLAB minres (SIRA_solve_residual_LS_GEP.m:54).
+// precision R, scalars in FP64.  The reference's SIRA inner solver is MATLAB
+// minres (SIRA_solve_residual_LS_GEP.m:54).
+//
+// The scalar recurrence runs on the device (two single-thread kernels per
+// iteration), every vector update reads its coefficients from device memory
+// and is masked by an `active` flag cleared at convergence, and the buffer
+// rotations are device copies.  An iteration is therefore a fixed launch
+// sequence: blocks of kMinresBlock iterations are captured once and replayed
+// from a CUDA graph, with one host check per block.
+namespace {
+
+constexpr int kMinresBlock = 8;
+
+// Scalar state of one MINRES solve (FP64, device).
+enum MrSlot {
+  MR_BETA = 0, MR_OLDB, MR_DBAR, MR_EPS, MR_PHIBAR, MR_CS, MR_SN, MR_TOLB,
+  MR_CV,        // 1 / beta               (v = y / beta)
+  MR_CR1,       // -beta / oldb           (y -= (beta/oldb) r1; 0 in the first step)
+  MR_CR2,       // -alfa / beta           (y -= (alfa/beta) r2)
+  MR_PHI,       // x += phi w
+  MR_W0, MR_W1, MR_W2,  // w = (v - oldeps w1 - delta w2) / gamma
+  MR_ONE, MR_ZERO, MR_NSLOT
+};
+struct MrInt {
+  int active, itn, nan;
+};
+
+__global__ void k_minres_alfa(double* S, const double2* __restrict__ dot, const MrInt* st) {
+  if (!st->active) return;
+  S[MR_CR2] = -dot->x / S[MR_BETA];
+}
+
+__global__ void k_minres_givens(double* S, const double2* __restrict__ alfa_dot, const double2* __restrict__ b2_dot,
+                                MrInt* st) {
+  if (!st->active) return;
+  const double alfa = alfa_dot->x, b2n = b2_dot->x;
+  st->itn += 1;
+  if (!isfinite(alfa) || !isfinite(b2n)) {
+    st->nan = 1;
+    st->active = 0;
+    return;
+  }
+  const double oldb = S[MR_BETA];
+  const double beta = sqrt(fmax(b2n, 0.0));
+  const double cs = S[MR_CS], sn = S[MR_SN], dbar = S[MR_DBAR];
+  const double oldeps = S[MR_EPS];
+  const double delta = cs * dbar + sn * alfa;
+  const double gbar = sn * dbar - cs * alfa;
+  S[MR_EPS] = sn * beta;
+  S[MR_DBAR] = -cs * beta;
+  const double gamma = fmax(sqrt(gbar * gbar + beta * beta), 1e-300);
+  const double cs2 = gbar / gamma, sn2 = beta / gamma;
+  S[MR_CS] = cs2;
+  S[MR_SN] = sn2;
+  S[MR_PHI] = cs2 * S[MR_PHIBAR];
+  S[MR_PHIBAR] = sn2 * S[MR_PHIBAR];
+  S[MR_W0] = 1.0 / gamma;
+  S[MR_W1] = -oldeps / gamma;
+  S[MR_W2] = -delta / gamma;
+  S[MR_OLDB] = oldb;
+  S[MR_BETA] = beta;
+  S[MR_CV] = beta > 0.0 ? 1.0 / beta : 0.0;
+  S[MR_CR1] = -beta / oldb;
+  if (S[MR_PHIBAR] <= S[MR_TOLB] || beta == 0.0) st->active = 2;  // converged: finish this step's updates
+}
+
+// out = S[ia] x + S[ib] y + S[ic] w (y, w may be null), only while active.
+template <class R>
+__global__ void k_lincomb_dev(cx<R>* __restrict__ out, const double* __restrict__ S, int ia, const cx<R>* x, int ib,
+                              const cx<R>* y, int ic, const cx<R>* w, long long len, const MrInt* __restrict__ st) {
+  if (!st->active) return;
+  const R a = R(S[ia]), b = R(S[ib]), c = R(S[ic]);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    cx<R> v = x[i];
+    R rx = a * v.x, ry = a * v.y;
+    if (y) {
+      const cx<R> u = y[i];
+      rx += b * u.x;
+      ry += b * u.y;
+    }
+    if (w) {
+      const cx<R> u = w[i];
+      rx += c * u.x;
+      ry += c * u.y;
+    }
+    out[i] = mk<R>(rx, ry);
+  }
+}
+
+// active 2 (converged during this step) -> 0 once the step's updates are done
+__global__ void k_minres_close(MrInt* st) {
+  if (st->active == 2) st->active = 0;
+}
+
+int lincomb_dev_grid(long long len) {
+  long long g = (len + 255) / 256;
+  return (int)std::min<long long>(g, 1216);
+}
+
+}  // namespace
+
 template <class R>
 int minres_shifted(Plan& P, const cx<R>* b, cx<R>* x, const int* d_inst, double shift, double tol, int maxit,
                    int* iters, double* relres) {
@@ -63,85 +164,132 @@ int minres_shifted(Plan& P, const cx<R>* b, cx<R>* x, const int* d_inst, double 
   JD_CK(e, "minres workspace");
   cx<R> *v = base, *y = base + L, *r1 = base + 2 * L, *r2 = base + 3 * L, *w = base + 4 * L, *w1 = base + 5 * L,
         *w2 = base + 6 * L, *ta = base + 7 * L;
-  double2* dd = (double2*)workspace(P, JD_R32 + 30, sizeof(double2) * (256 + 4), &e);
+  char* sm = (char*)workspace(P, JD_R32 + 30, sizeof(double2) * (3 * 256 + 8) + sizeof(double) * MR_NSLOT + 64, &e);
   JD_CK(e, "minres workspace");
+  double2* part = (double2*)sm;          // dot partials
+  double2* dalfa = part + 256;           // v . y
+  double2* db2 = dalfa + 1;              // |r2|^2
+  double2* dbb = db2 + 1;                // |b|^2
+  double* S = (double*)(dbb + 5);
+  MrInt* SI = (MrInt*)(S + MR_NSLOT);
   JD_CK(ensure_work(P, 1), "minres scratch");
   VecCtx c1;
   c1.inst = d_inst;
   c1.nk = P.nk;
-  auto op = [&](const cx<R>* in, cx<R>* out) -> cudaError_t {  // out = B in - shift A in
+  c1.active = &SI->active;  // the operator's kernels skip once converged
+  const int gl = lincomb_dev_grid(L);
+  auto lc = [&](cudaStream_t cs, cx<R>* out, int ia, const cx<R>* xx, int ib, const cx<R>* yy, int ic,
+                const cx<R>* ww) -> cudaError_t {
+    FAME_LAUNCHED(1);
+    k_lincomb_dev<R><<<gl, 256, 0, cs>>>(out, S, ia, xx, ib, yy, ic, ww, L, SI);
+    return cudaGetLastError();
+  };
+  auto op = [&](cudaStream_t cs, const cx<R>* in, cx<R>* out) -> cudaError_t {  // out = B in - shift A in
     cx<R>* w0 = (cx<R>*)P.d_work;
-    cudaError_t e2 = launch_fncB<R>(P, in, out, 1, c1, w0, w0 + 6 * P.Nq, st);
+    cudaError_t e2 = launch_fncB<R>(P, in, out, 1, c1, w0, w0 + 6 * P.Nq, cs);
     if (e2 != cudaSuccess || shift == 0.0) return e2;
-    e2 = launch_fncA<R>(P, in, ta, 1, c1, st);
+    e2 = launch_fncA<R>(P, in, ta, 1, c1, cs);
     if (e2 != cudaSuccess) return e2;
-    return lincomb3<R>(out, 1.0, out, -shift, ta, 0.0, nullptr, L, st);
+    return lincomb3<R>(out, 1.0, out, -shift, ta, 0.0, nullptr, L, cs);
   };
-  auto dot = [&](const cx<R>* a, const cx<R>* bb, double* re) -> int {
-    JD_CK(dot_batched<R>(a, 0, 0, 1, bb, 0, L, 1, dd + 256, dd, 256, nullptr, st), "minres dot");
-    double2 h;
-    JD_CK(cudaMemcpyAsync(&h, dd + 256, sizeof(double2), cudaMemcpyDeviceToHost, st), "minres dot");
-    JD_CK(cudaStreamSynchronize(st), "minres dot");
-    *re = h.x;
-    return FAME_OK;
+  // one MINRES step (Paige-Saunders), every scalar on the device
+  auto step = [&](cudaStream_t cs) -> cudaError_t {
+    cudaError_t e2 = lc(cs, v, MR_CV, y, MR_ZERO, nullptr, MR_ZERO, nullptr);     // v = y / beta
+    if (e2 == cudaSuccess) e2 = op(cs, v, y);                                      // y = (B - shift A) v
+    if (e2 == cudaSuccess) e2 = lc(cs, y, MR_ONE, y, MR_CR1, r1, MR_ZERO, nullptr);  // y -= (beta/oldb) r1
+    if (e2 == cudaSuccess) e2 = dot_batched<R>(v, 0, 0, 1, y, 0, L, 1, dalfa, part, 256, &SI->active, cs);
+    if (e2 == cudaSuccess) {
+      FAME_LAUNCHED(1);
+      k_minres_alfa<<<1, 1, 0, cs>>>(S, dalfa, SI);
+      e2 = cudaGetLastError();
+    }
+    if (e2 == cudaSuccess) e2 = lc(cs, y, MR_ONE, y, MR_CR2, r2, MR_ZERO, nullptr);  // y -= (alfa/beta) r2
+    if (e2 == cudaSuccess) e2 = lc(cs, r1, MR_ONE, r2, MR_ZERO, nullptr, MR_ZERO, nullptr);  // r1 <- r2
+    if (e2 == cudaSuccess) e2 = lc(cs, r2, MR_ONE, y, MR_ZERO, nullptr, MR_ZERO, nullptr);   // r2 <- y
+    if (e2 == cudaSuccess) e2 = dot_batched<R>(r2, 0, 0, 1, r2, 0, L, 1, db2, part, 256, &SI->active, cs);
+    if (e2 == cudaSuccess) {
+      FAME_LAUNCHED(1);
+      k_minres_givens<<<1, 1, 0, cs>>>(S, dalfa, db2, SI);
+      e2 = cudaGetLastError();
+    }
+    if (e2 == cudaSuccess) e2 = lc(cs, w1, MR_ONE, w2, MR_ZERO, nullptr, MR_ZERO, nullptr);  // w1 <- w2
+    if (e2 == cudaSuccess) e2 = lc(cs, w2, MR_ONE, w, MR_ZERO, nullptr, MR_ZERO, nullptr);   // w2 <- w
+    if (e2 == cudaSuccess) e2 = lc(cs, w, MR_W0, v, MR_W1, w1, MR_W2, w2);      // w = (v - e w1 - d w2)/g
+    if (e2 == cudaSuccess) e2 = lc(cs, x, MR_ONE, x, MR_PHI, w, MR_ZERO, nullptr);  // x += phi w
+    if (e2 == cudaSuccess) {
+      FAME_LAUNCHED(1);
+      k_minres_close<<<1, 1, 0, cs>>>(SI);
+      e2 = cudaGetLastError();
+    }
+    return e2;
   };
+
   JD_CK(cudaMemsetAsync(x, 0, vb, st), "minres init");
   JD_CK(cudaMemsetAsync(w, 0, vb, st), "minres init");
   JD_CK(cudaMemsetAsync(w2, 0, vb, st), "minres init");
-  JD_CK(cudaMemcpyAsync(r1, b, vb, cudaMemcpyDeviceToDevice, st), "minres init");
+  JD_CK(cudaMemsetAsync(r1, 0, vb, st), "minres init");
   JD_CK(cudaMemcpyAsync(r2, b, vb, cudaMemcpyDeviceToDevice, st), "minres init");
   JD_CK(cudaMemcpyAsync(y, b, vb, cudaMemcpyDeviceToDevice, st), "minres init");
-  double b2;
-  int rc = dot(b, b, &b2);
-  if (rc) return rc;
-  if (!std::isfinite(b2)) return fail(&P, FAME_ERR_NAN, "minres: non-finite right-hand side");
-  const double beta1 = std::sqrt(std::max(b2, 0.0));
+  JD_CK(dot_batched<R>(b, 0, 0, 1, b, 0, L, 1, dbb, part, 256, nullptr, st), "minres dot");
+  double2 hb;
+  JD_CK(cudaMemcpyAsync(&hb, dbb, sizeof(double2), cudaMemcpyDeviceToHost, st), "minres dot");
+  JD_CK(cudaStreamSynchronize(st), "minres dot");
+  if (!std::isfinite(hb.x)) return fail(&P, FAME_ERR_NAN, "minres: non-finite right-hand side");
+  const double beta1 = std::sqrt(std::max(hb.x, 0.0));
   if (beta1 == 0.0) {
     if (iters) *iters = 0;
     if (relres) *relres = 0.0;
     return FAME_OK;
   }
-  double oldb = 0.0, beta = beta1, dbar = 0.0, epsln = 0.0, phibar = beta1, cs = -1.0, sn = 0.0;
-  int itn = 0;
-  double rnorm = beta1;
-  for (itn = 1; itn <= maxit; ++itn) {
-    const double s = 1.0 / beta;
-    JD_CK(lincomb3<R>(v, s, y, 0.0, nullptr, 0.0, nullptr, L, st), "minres");
-    JD_CK(op(v, y), "minres op");
-    if (itn >= 2) JD_CK(lincomb3<R>(y, 1.0, y, -beta / oldb, r1, 0.0, nullptr, L, st), "minres");
-    double alfa;
-    if ((rc = dot(v, y, &alfa))) return rc;
-    JD_CK(lincomb3<R>(y, 1.0, y, -alfa / beta, r2, 0.0, nullptr, L, st), "minres");
-    std::swap(r1, r2);                                   // r1 <- r2
-    JD_CK(cudaMemcpyAsync(r2, y, vb, cudaMemcpyDeviceToDevice, st), "minres");  // r2 <- y
-    oldb = beta;
-    double b2n;
-    if ((rc = dot(r2, r2, &b2n))) return rc;
-    if (!std::isfinite(b2n) || !std::isfinite(alfa)) return fail(&P, FAME_ERR_NAN, "minres: non-finite value");
-    beta = std::sqrt(std::max(b2n, 0.0));
-    const double oldeps = epsln;
-    const double delta = cs * dbar + sn * alfa;
-    const double gbar = sn * dbar - cs * alfa;
-    epsln = sn * beta;
-    dbar = -cs * beta;
-    double gamma = std::sqrt(gbar * gbar + beta * beta);
-    gamma = std::max(gamma, 1e-300);
-    cs = gbar / gamma;
-    sn = beta / gamma;
-    const double phi = cs * phibar;
-    phibar = sn * phibar;
-    const double denom = 1.0 / gamma;
-    std::swap(w1, w2);  // w1 <- w2 (old w1 becomes scratch)
-    std::swap(w2, w);   // w2 <- w
-    // w = (v - oldeps w1 - delta w2) / gamma
-    JD_CK(lincomb3<R>(w, denom, v, -oldeps * denom, w1, -delta * denom, w2, L, st), "minres");
-    JD_CK(lincomb3<R>(x, 1.0, x, phi, w, 0.0, nullptr, L, st), "minres");
-    rnorm = phibar;
-    if (rnorm <= tol * beta1 || beta == 0.0) break;
+  double hs[MR_NSLOT] = {};
+  hs[MR_BETA] = beta1;
+  hs[MR_OLDB] = 0.0;
+  hs[MR_PHIBAR] = beta1;
+  hs[MR_CS] = -1.0;
+  hs[MR_SN] = 0.0;
+  hs[MR_TOLB] = tol * beta1;
+  hs[MR_CV] = 1.0 / beta1;
+  hs[MR_CR1] = 0.0;
+  hs[MR_ONE] = 1.0;
+  hs[MR_ZERO] = 0.0;
+  MrInt hi{1, 0, 0};
+  JD_CK(h2d_async(P, S, hs, sizeof(hs)), "minres init");
+  JD_CK(h2d_async(P, SI, &hi, sizeof(hi)), "minres init");
+  uint64_t shift_bits;
+  std::memcpy(&shift_bits, &shift, sizeof(shift));
+  const std::vector<uintptr_t> gkey = {0x4d52u, sizeof(R), (uintptr_t)P.n, (uintptr_t)base, (uintptr_t)sm,
+                                       (uintptr_t)x, (uintptr_t)d_inst, (uintptr_t)P.d_work, (uintptr_t)shift_bits,
+                                       (uintptr_t)kMinresBlock};
+  bool use_graph = P.opt_graph != 0;
+  MrInt hst = hi;
+  double phibar = beta1;
+  int done_steps = 0;
+  while (done_steps < maxit) {
+    const int nb = std::min(kMinresBlock, maxit - done_steps);
+    bool issued = false;
+    if (use_graph && nb == kMinresBlock) {
+      cudaError_t ge = graph_replay(P, gkey, [&](cudaStream_t cs) -> cudaError_t {
+        for (int i = 0; i < kMinresBlock; ++i) {
+          cudaError_t e2 = step(cs);
+          if (e2 != cudaSuccess) return e2;
+        }
+        return cudaSuccess;
+      });
+      if (ge == cudaSuccess) issued = true;
+      else use_graph = false;
+    }
+    if (!issued)
+      for (int i = 0; i < nb; ++i) JD_CK(step(st), "minres step");
+    done_steps += nb;
+    JD_CK(cudaMemcpyAsync(&hst, SI, sizeof(MrInt), cudaMemcpyDeviceToHost, st), "minres check");
+    JD_CK(cudaMemcpyAsync(&phibar, S + MR_PHIBAR, sizeof(double), cudaMemcpyDeviceToHost, st), "minres check");
+    JD_CK(cudaStreamSynchronize(st), "minres check");
+    if (hst.nan) return fail(&P, FAME_ERR_NAN, "minres: non-finite value");
+    if (!hst.active) break;
   }
-  if (iters) *iters = std::min(itn, maxit);
-  if (relres) *relres = rnorm / beta1;
-  return rnorm <= tol * beta1 ? FAME_OK : FAME_ERR_NOT_CONVERGED;
+  if (iters) *iters = hst.itn;
+  if (relres) *relres = phibar / beta1;
+  return phibar <= tol * beta1 ? FAME_OK : FAME_ERR_NOT_CONVERGED;
 }
 
 template int minres_shifted<float>(Plan&, const float2*, float2*, const int*, double, double, int, int*, double*);
