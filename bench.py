@@ -135,6 +135,13 @@ class Clocks:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
+def workload_config(batch):
+    """The benchmark workload, shared by both arms' JSON lines."""
+    return {"workload": "woodpile n=60 (FCC a=1, rod width 0.25a, eps=13, xi=-zeta=0.2i), "
+                        "40-point path G-X-U|K-G-L-W-X, 10 bands, Lanczos tol 1e-10, res<=1e-8",
+            "n": N_GRID, "bands": BANDS, "kpoints_per_step": batch, "path_kpoints": PATH_POINTS}
+
+
 def path_batches(batch):
     import fame
 
@@ -289,12 +296,11 @@ def run_fame(args):
             "warmup": args.warmup, "ms_per_step": round(tmax / args.steps * 1e3, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64/f64", "data": "synthetic (woodpile geometry, "
             "band path generated in-run)",
-            "config": {"workload": "woodpile n=60 (FCC a=1, rod width 0.25a, eps=13, xi=-zeta=0.2i), "
-                                   "40-point path G-X-U|K-G-L-W-X, 10 bands, Lanczos tol 1e-10, res<=1e-8",
-                       "n": N_GRID, "bands": BANDS, "lanczos_p": LANCZOS_P_MIXED, "kpoints_per_step": args.batch, "path_kpoints": PATH_POINTS,
-                       "precision": "complex64 fncB + preconditioned CG, FP64 recurrence/reorth/residual "
-                                    f"refinement (B^-1 to {INNER_TOL_MIXED:g}, tighter near Gamma)/NFSEP check",
-                       "l2": "inputs larger than L2 (Lanczos basis and B*Q of a batch ~5.3 GB)"},
+            "config": dict(workload_config(args.batch),
+                           lanczos_p=LANCZOS_P_MIXED,
+                           precision="complex64 fncB + preconditioned CG, FP64 recurrence/reorth/residual "
+                                     f"refinement (B^-1 to {INNER_TOL_MIXED:g}, tighter near Gamma)/NFSEP check",
+                           l2="inputs larger than L2 (Lanczos basis and B*Q of a batch ~5.3 GB)"),
             "e2e": {"value": None if e2e_value is None else round(e2e_value, 5), "unit": UNIT,
                     "h2d_bytes_per_step": int(h2d / max(1, e2e_steps)),
                     "d2h_bytes_per_step": int(d2h / max(1, e2e_steps)), "steps": e2e_steps,
@@ -332,7 +338,8 @@ def cpu_baseline(seconds, b_applies):
         P.B(x)
         cnt += 1
     tb = (time.perf_counter() - t0) / cnt
-    return {"value": round(1.0 / (tb * b_applies), 8), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+    import oracle as O
+    return {"value": round(1.0 / (tb * b_applies), 8), "unit": UNIT, "cores": O.fft_workers(), "kind": "port",
             "sample": f"{cnt} FP64 oracle fncB applications at n=60 (X point), {tb * 1e3:.1f} ms each; one "
                       f"k-point solve extrapolated as {b_applies:.0f} applications (FP64 Lanczos + CG count)"}
 
@@ -341,6 +348,8 @@ def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return
+    import oracle as O
+    threads = O.fft_workers()  # FFT threads; the sparse material products run on one
     P = _oracle_problem()
     x = np.ones(4 * N_GRID ** 3, dtype=np.complex128)
     for _ in range(args.warmup):
@@ -360,9 +369,11 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(tb * per * 1e3, 2), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-        "config": {"workload": "woodpile n=60, 10 bands, Lanczos tol 1e-10 (CPU restatement of the MATLAB "
-                               "path; MATLAB unavailable on this box)", "n": N_GRID, "bands": BANDS},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": sample},
+        "config": dict(workload_config(args.batch),
+                       lanczos_p=2 * BANDS,
+                       precision="FP64 throughout, unpreconditioned pcg to 1e-12 (the reference's algorithm, "
+                                 "restated on the CPU; MATLAB unavailable on this box)"),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
