@@ -335,6 +335,10 @@ int fame_set_option(fame_plan_t h, int option, double value) {
     case FAME_OPT_GRAPH:
       P.opt_graph = value != 0.0;
       return FAME_OK;
+    case FAME_OPT_ITOL_FLOOR:
+      if (!(value > 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: itol floor in (0, 1)");
+      P.opt_itol_floor = value;
+      return FAME_OK;
     case FAME_OPT_TOL32:
       if (!(value > 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: tol32 in (0,1)");
       P.opt_tol32 = value;

@@ -81,6 +81,7 @@ struct Plan {
   int opt_precond = 1;                // CG on B preconditioned by the averaged-medium B0^{-1}
   double opt_tol32 = 1e-6;            // complex64 CG tolerance of the first refinement round
   int opt_graph = 1;                  // replay CG iterations from captured CUDA graphs
+  double opt_itol_floor = 1e-13;      // mixed form: floor of the spread-scaled inner tolerance
   std::vector<double> theta;          // [nk][3]
   std::vector<double> sigma_min;      // [nk] smallest curl singular value sqrt(min |L|^2)
   std::vector<double> mat_avg;        // [nk][27][2] volume-averaged Herm(N) | Herm(M) | J

@@ -379,9 +379,11 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     if (prec == FAME_C64 && P.sigma_min[insts[a]] < 1e-2) {
       // A near-zero wave vector (Gamma shifted by 1e-4) gives curl singular
       // values ~1e-4 and eigenvalues lambda ~ 1e4 among the wanted ones: run
-      // this instance with the tightest inner solves and explicit FP64 B r
-      // from the first step (see the spread rule at the restarts).
-      S[a].itol = 1e-15;
+      // this instance at the inner-tolerance floor with explicit FP64 B r
+      // from the first step (see the spread rule at the restarts).  At n = 60
+      // a floor of 1e-13 leaves NFSEP residuals ~3e-11 there; 1e-12 does not
+      // reach 1e-8.
+      S[a].itol = P.opt_itol_floor;
       S[a].explicit_br = true;
     }
   }
@@ -655,7 +657,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         // tolerance by the spread of the wanted Ritz values.
         const double lmax = std::fabs(w[ind[0]]), lk = std::fabs(w[ind[I.k0 - 1]]);
         const double spread = lmax > 0.0 ? std::min(1.0, lk / lmax) : 1.0;
-        I.itol = std::max(1e-15, itol * spread);
+        I.itol = std::max(P.opt_itol_floor, itol * spread);
         I.refresh_bq = !I.explicit_br && spread < 1e-3;
         I.explicit_br = spread < 1e-3;
       }

@@ -28,6 +28,7 @@ FAME_HOST_PTR = 1
 FAME_OPT_PRECOND = 0
 FAME_OPT_TOL32 = 1
 FAME_OPT_GRAPH = 2
+FAME_OPT_ITOL_FLOOR = 3
 
 STATUS_NAMES = {0: "OK", 1: "BAD_ARG", 2: "CUDA", 3: "NOT_CONVERGED", 4: "BREAKDOWN", 5: "NAN",
                 6: "UNSUPPORTED", 7: "SINGULAR", 8: "ALLOC"}

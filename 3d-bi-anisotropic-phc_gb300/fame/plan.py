@@ -207,8 +207,9 @@ class Plan:
         check(self._lib.fame_sync(self._h), self._h, "fame_sync")
 
     def set_option(self, option, value):
-        """fame_set_option: 'precond' (bool), 'tol32' (float) or 'graph' (bool)."""
-        code = {"precond": L.FAME_OPT_PRECOND, "tol32": L.FAME_OPT_TOL32, "graph": L.FAME_OPT_GRAPH}.get(option, option)
+        """fame_set_option: 'precond' (bool), 'tol32' (float), 'graph' (bool) or 'itol_floor' (float)."""
+        code = {"precond": L.FAME_OPT_PRECOND, "tol32": L.FAME_OPT_TOL32, "graph": L.FAME_OPT_GRAPH,
+                "itol_floor": L.FAME_OPT_ITOL_FLOOR}.get(option, option)
         check(self._lib.fame_set_option(self._h, int(code), float(value)), self._h, "fame_set_option")
         return self
 

@@ -81,8 +81,12 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *   FAME_OPT_TOL32    complex64 CG tolerance of the first refinement round of
  *                     the mixed-precision B^{-1} [1e-6].
  *   FAME_OPT_GRAPH    replay blocks of CG iterations from CUDA graphs captured
- *                     on first use [1]; 0 launches every kernel directly. */
-enum fame_option { FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2 };
+ *                     on first use [1]; 0 launches every kernel directly.
+ *   FAME_OPT_ITOL_FLOOR  mixed form: lower bound of the per-instance inner
+ *                     tolerance, which is tightened by the spread of the
+ *                     wanted Ritz values and starts there at near-zero wave
+ *                     vectors [1e-13]. */
+enum fame_option { FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2, FAME_OPT_ITOL_FLOOR = 3 };
 int fame_set_option(fame_plan_t plan, int option, double value);
 
 /*
