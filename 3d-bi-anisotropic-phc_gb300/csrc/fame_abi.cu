@@ -15,8 +15,15 @@
 
 namespace fame {
 
+// Error text of calls that have no plan to hold it (per thread: plans may be
+// created from several threads at once).
+static thread_local std::string g_static_error;
+
 int fail(Plan* P, int code, const std::string& msg) {
-  if (P) P->last_error = msg;
+  if (P)
+    P->last_error = msg;
+  else
+    g_static_error = msg;
   return code;
 }
 
@@ -29,9 +36,6 @@ template <class R> PlanData<R>& pdata_mut(Plan& P);
 template <> PlanData<double>& pdata_mut<double>(Plan& P) { return P.d64; }
 template <> PlanData<float>& pdata_mut<float>(Plan& P) { return P.d32; }
 
-// Error text of calls that have no plan to hold it (per thread: plans may be
-// created from several threads at once).
-static thread_local std::string g_static_error;
 unsigned long long g_kernel_launches = 0;
 
 void* workspace(Plan& P, int id, size_t bytes, cudaError_t* err) {

@@ -11,6 +11,6 @@ from . import adjoint  # noqa: F401
 from .handles import Lanczos, Lanczos_gep, MtxVecMul_FFT, fncA, fncB, fncinvB, woodpile_plan  # noqa: F401
 from .plan import Plan  # noqa: F401
 from .setup import (band_path, bi_isotropic, bloch_angles, constitutive, covariant_blocks,  # noqa: F401
-                    fcc_lattice, fcc_point, reference_path, sphere_inside, tetra_inside, vertex_positions,
+                    fcc_lattice, fcc_point, rasterize, reference_path, sphere_inside, tetra_inside, vertex_positions,
                     woodpile_inside)
 from . import interior  # noqa: F401

@@ -29,6 +29,8 @@ FAME_OPT_PRECOND = 0
 FAME_OPT_TOL32 = 1
 FAME_OPT_GRAPH = 2
 FAME_OPT_ITOL_FLOOR = 3
+FAME_SHAPE_WOODPILE, FAME_SHAPE_SPHERE, FAME_SHAPE_TETRA = 0, 1, 2
+FAME_RASTER_PAINT = 2
 
 STATUS_NAMES = {0: "OK", 1: "BAD_ARG", 2: "CUDA", 3: "NOT_CONVERGED", 4: "BREAKDOWN", 5: "NAN",
                 6: "UNSUPPORTED", 7: "SINGULAR", 8: "ALLOC"}
@@ -69,6 +71,7 @@ SIGNATURES = {
     "fame_restore": (_i, [_vp, _i, _pi, _vp, _pd, _vp, _vp, _pd, _pd, _pd, _i]),
     "fame_autotune": (_i, [_vp, _i, _i, _pi, _pi, _pd]),
     "fame_set_tune": (_i, [_vp, _i, _i, _i, _i]),
+    "fame_rasterize": (_i, [_i, _pd, _i, _pd, _i, _vp, _i]),
 }
 
 

@@ -10,7 +10,7 @@ import numpy as np
 
 from . import _lib as L
 from .plan import Plan
-from .setup import bi_isotropic, bloch_angles, fcc_lattice, vertex_positions, woodpile_inside
+from .setup import bi_isotropic, bloch_angles, fcc_lattice, rasterize
 
 
 def fncA(x, plan: Plan, inst=None):
@@ -164,8 +164,7 @@ def woodpile_plan(n: int, wave_vecs, gamma=0.2, eps_in=13.0, width=0.25, gammas=
     A = fcc_lattice()
     kv = np.atleast_2d(np.asarray(wave_vecs, dtype=np.float64))
     th = np.stack([bloch_angles(k, A) for k in kv])
-    inside = woodpile_inside(vertex_positions(n, A), width)
-    phase = inside.astype(np.uint8)
+    phase = rasterize(n, "woodpile", width, A)
     vac = bi_isotropic(1.0, 0.0)
     if gammas is None:
         return Plan.from_phases(n, th, phase, [vac, bi_isotropic(eps_in, gamma)], A)

@@ -20,7 +20,7 @@ import time
 import numpy as np
 
 from .plan import Plan
-from .setup import bi_isotropic, bloch_angles, fcc_lattice, sphere_inside, tetra_inside, vertex_positions
+from .setup import bi_isotropic, bloch_angles, fcc_lattice, rasterize
 
 try:
     import torch
@@ -33,16 +33,15 @@ def inclusion_plan(n, wave_vecs, shape="sphere", gamma=0.5, eps_in=13.0, size=No
     sphere (radius `size`, default 0.25a) or regular tetrahedron (edge `size`,
     default 0.5a) at the cell origin; one instance per wave vector."""
     A = fcc_lattice()
-    P = vertex_positions(n, A)
     if shape == "sphere":
-        inside = sphere_inside(P, 0.25 if size is None else size, A)
+        phase = rasterize(n, "sphere", 0.25 if size is None else size, A)
     elif shape in ("tetra", "tri", "tetrahedron"):
-        inside = tetra_inside(P, 0.5 if size is None else size, A)
+        phase = rasterize(n, "tetra", 0.5 if size is None else size, A)
     else:
         raise ValueError(shape)
     kv = np.atleast_2d(np.asarray(wave_vecs, dtype=np.float64))
     th = np.stack([bloch_angles(k, A) for k in kv])
-    return Plan.from_phases(n, th, inside.astype(np.uint8), [bi_isotropic(1.0, 0.0), bi_isotropic(eps_in, gamma)], A)
+    return Plan.from_phases(n, th, phase, [bi_isotropic(1.0, 0.0), bi_isotropic(eps_in, gamma)], A)
 
 
 def band_edge(plan, band=4, tol=1e-10, prec="c64"):

@@ -247,6 +247,13 @@ class Plan:
             os.replace(tmp, cache)
         return dict(t, cached=False)
 
+    def set_tune(self, prec, nvec, chunk, stencil_tpb):
+        """fame_set_tune: install fncB launch parameters measured before (on
+        another plan of the same grid, precision and batch width)."""
+        pr = L.FAME_C64 if prec in ("c64", L.FAME_C64) else L.FAME_C128
+        check(self._lib.fame_set_tune(self._h, pr, int(nvec), int(chunk), int(stencil_tpb)), self._h,
+              "fame_set_tune")
+
     # -- generic call -------------------------------------------------------
     def _call(self, fn, x, out_len, inst, *extra, name=""):
         prec = _prec_of(x)

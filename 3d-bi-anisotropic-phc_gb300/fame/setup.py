@@ -14,6 +14,11 @@ import numpy as np
 
 from ._lib import check, load
 
+try:
+    import torch
+except ImportError:  # pragma: no cover
+    torch = None
+
 # FCC high-symmetry points in reciprocal-lattice coordinates
 # (InputData/BS_Gyroid/Physical_settings_woodpile.m:143-148)
 FCC_POINTS = {
@@ -207,3 +212,52 @@ def covariant_blocks(c6: np.ndarray, A: np.ndarray | None = None) -> np.ndarray:
     check(lib.fame_material_blocks(c6.view(np.float64).ctypes.data_as(pd), lat.ctypes.data_as(pd),
                                    out.ctypes.data_as(pd)), None, "fame_material_blocks")
     return out.view(np.complex128).copy()
+
+
+SHAPES = {"woodpile": 0, "sphere": 1, "tetra": 2, "tetrahedron": 2, "tri": 2}
+
+
+def rasterize(n: int, shape: str, size: float, A: np.ndarray | None = None, center=(0.0, 0.0, 0.0),
+              a: float = 1.0, phase_id: int = 1, phase=None, device: bool = False):
+    """Phase id of every vertex of the n^3 grid from the device rasteriser
+    (fame_rasterize): `phase_id` inside the shape, 0 outside, or the id
+    already in `phase` when it is given (several inclusions).
+
+    shape 'woodpile': rod width `size`, lattice constant `a`
+    (Public/woodpile_isofun.m); 'sphere': radius `size` about `center`
+    (Physical_settings_sphere.m:18); 'tetra': regular tetrahedron of edge
+    `size` about `center` (Material_Locate_Isofunction.m:135-148).  Sphere and
+    tetrahedron include their 27 periodic images.  Returns a uint8 numpy array,
+    or a CUDA uint8 tensor when `device` (or when `phase` is one)."""
+    A = fcc_lattice() if A is None else A
+    lib = load()
+    kind = SHAPES[shape]
+    if kind == 0:
+        params = np.array([size, a], dtype=np.float64)
+    else:
+        params = np.array([size, *np.asarray(center, dtype=np.float64)], dtype=np.float64)
+    lat = np.ascontiguousarray(A, dtype=np.float64)
+    pd = C.POINTER(C.c_double)
+    Nq = n ** 3
+    flags = 2 if phase is not None else 0
+    on_device = device or (torch is not None and isinstance(phase, torch.Tensor))
+    if on_device:
+        if phase is None:
+            out = torch.empty(Nq, dtype=torch.uint8, device="cuda")
+        else:
+            out = phase
+            if out.dtype != torch.uint8 or not out.is_cuda or not out.is_contiguous() or out.numel() != Nq:
+                raise ValueError("phase must be a contiguous CUDA uint8 tensor of n^3 elements")
+        ptr = C.c_void_p(out.data_ptr())
+    else:
+        if phase is None:
+            out = np.zeros(Nq, dtype=np.uint8)
+        else:
+            out = np.ascontiguousarray(phase, dtype=np.uint8).reshape(-1)
+            if out.size != Nq:
+                raise ValueError("phase must hold n^3 ids")
+        flags |= 1
+        ptr = C.c_void_p(out.ctypes.data)
+    check(lib.fame_rasterize(int(n), lat.ctypes.data_as(pd), kind, params.ctypes.data_as(pd), int(phase_id), ptr,
+                             flags), None, "fame_rasterize")
+    return out

@@ -251,6 +251,31 @@ int fame_eig_gradient(fame_plan_t plan, int nvec, const int* inst, const void* x
  */
 int fame_material_blocks(const double* eps_xi_zeta_mu, const double* lattice, double* out);
 
+/*
+ * Vertex rasterisation of one inclusion on the device: every vertex of the
+ * n^3 grid (lattice coefficients (i-1)/n, Public/Grid_Generate_Mult_Point.m:7-17)
+ * inside the shape gets phase id `id`; the others get 0, or keep their id
+ * when `flags` has FAME_RASTER_PAINT (several inclusions, the union of
+ * Material_Locate_Isofunction.m:22-25).  phase [n^3], x fastest, device
+ * memory unless `flags` has FAME_HOST_PTR.  lattice: 3x3 row-major, columns
+ * are the primitive vectors.  Shapes and params:
+ *   FAME_SHAPE_WOODPILE  {width, a}: Public/woodpile_isofun.m:1-13;
+ *   FAME_SHAPE_SPHERE    {radius, cx, cy, cz}: -min_c |r - c| > -radius over
+ *                        the 27 periodic images of the centre
+ *                        (Physical_settings_sphere.m:18);
+ *   FAME_SHAPE_TETRA     {edge, cx, cy, cz}: regular tetrahedron with
+ *                        vertices along (1,1,1), (1,-1,-1), (-1,1,-1),
+ *                        (-1,-1,1), inside when on the opposite vertex's side
+ *                        of every face or within 1e-8 of it
+ *                        (Material_Locate_Isofunction.m:135-148), 27 images.
+ * Synchronous.  Replaces the host-side point location of
+ * subroutines/Material_Locate_Isofunction.m:1-28.
+ */
+enum fame_shape { FAME_SHAPE_WOODPILE = 0, FAME_SHAPE_SPHERE = 1, FAME_SHAPE_TETRA = 2 };
+#define FAME_RASTER_PAINT 2
+int fame_rasterize(int n, const double* lattice, int shape, const double* params, int id, uint8_t* phase,
+                   int flags);
+
 #ifdef __cplusplus
 }
 #endif
