@@ -1,9 +1,10 @@
 // Autotuner of the fncB launch sequence: times the candidate launch
 // parameters on the plan's own grid, instances and batch width and keeps the
 // fastest per (precision, batch width).  Knobs:
-//   chunk        vectors per launch sequence (whole batch, 1/2, 1/4, 1/8):
-//                smaller sub-batches keep the six-field intermediates in L2
-//                at the cost of smaller grids;
+//   chunk        vectors per launch sequence (whole batch, 1/2, 1/4, 1/8,
+//                any width up to 16): smaller sub-batches keep the six-field
+//                intermediates in L2, and some widths fill the last wave of
+//                CTAs better than others;
 //   stencil_tpb  threads per block of the two stencil kernels (128/256/512).
 // No counterpart in the reference.
 #include <algorithm>
@@ -47,11 +48,16 @@ static int autotune_prec(Plan& P, int nvec, int reps, TuneEntry* best_out) {
   cx<R>* w1 = w0 + (size_t)nvec * 6 * P.Nq;
   VecCtx ctx;
   ctx.nk = P.nk;
+  // The whole batch, halves, quarters and eighths, and every width up to 16:
+  // the plane kernels launch 2n CTAs per vector, and how well a width fills
+  // the last wave of resident CTAs (2 per SM at n = 60) matters as much as
+  // L2 residency.
   std::vector<int> chunks;
-  for (int div : {1, 2, 4, 8}) {
-    const int c = (nvec + div - 1) / div;
-    if (c >= 1 && std::find(chunks.begin(), chunks.end(), c) == chunks.end()) chunks.push_back(c);
-  }
+  auto add = [&](int c) {
+    if (c >= 1 && c <= nvec && std::find(chunks.begin(), chunks.end(), c) == chunks.end()) chunks.push_back(c);
+  };
+  for (int div : {1, 2, 4, 8}) add((nvec + div - 1) / div);
+  for (int c = 1; c <= 16; ++c) add(c);
   const int prec = sizeof(R) == 4 ? FAME_C64 : FAME_C128;
   const TuneEntry saved = tune_for(P, prec, nvec);
   cudaEvent_t ev[2];

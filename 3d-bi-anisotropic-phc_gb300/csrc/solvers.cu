@@ -2,6 +2,7 @@
 // (fncinvB), the mixed-precision B^{-1} used by the complex64 band solve,
 // and the thick-restart Lanczos band solver of fun_Lanczos/Lanczos.m.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -29,8 +30,22 @@ enum WsId {
     if (e_ != cudaSuccess) return cuda_fail(&P, e_, where); \
   } while (0)
 
-static int dot_blocks(long long len, int nvec) {
-  long long target = (4LL * 152 + nvec - 1) / std::max(1, nvec);
+static int device_sms(int dev) {
+  static std::atomic<int> cache[64];
+  if (dev < 0 || dev >= 64) dev = 0;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+    cache[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
+
+// CTAs per vector of the grid-stride reduction and update kernels: together
+// at most four per SM (one wave at four resident CTAs, two at two), so that
+// no CTA of a batch waits for a partial last wave.
+static int dot_blocks(const Plan& P, long long len, int nvec) {
+  long long target = std::max(1, 4 * device_sms(P.device) / std::max(1, nvec));
   long long maxb = (len + 2047) / 2048;
   long long b = std::min(target, maxb);
   if (b < 1) b = 1;
@@ -71,7 +86,7 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
   S.res2 = S.tol2b2 + nvec;
   S.active = (int*)(S.res2 + nvec);
   S.iters = S.active + nvec;
-  const int nblk = dot_blocks(L, nvec);
+  const int nblk = dot_blocks(P, L, nvec);
   double2* part = (double2*)workspace(P, WS_PCG_PART, sizeof(double2) * nblk * nvec + 64, &e);
   FAME_CK(e, "pcg workspace");
   FAME_CK(ensure_work(P, nvec), "pcg fncB scratch");
@@ -116,7 +131,7 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
   // Preconditioned CG (M = B0^{-1}, precond.cu) or plain CG as in fncinvB.m.
   const bool pre = P.opt_precond != 0;
   cx<R>* z = nullptr;
-  const int nblkv = dot_blocks(P.Nq, nvec);  // per-voxel fused kernels
+  const int nblkv = dot_blocks(P, P.Nq, nvec);  // per-voxel fused kernels
   if (pre) {
     z = (cx<R>*)workspace(P, WS_PCG_Z + (sizeof(R) == 4 ? 100 : 0), vb, &e);
     FAME_CK(e, "pcg workspace");
@@ -220,7 +235,7 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
   FAME_CK(e, "mixed workspace");
   double2* res = (double2*)workspace(P, WS_MIX_RES, sizeof(double2) * L * nvec, &e);
   FAME_CK(e, "mixed workspace");
-  const int nblk = dot_blocks(L, nvec);
+  const int nblk = dot_blocks(P, L, nvec);
   char* sc = (char*)workspace(P, WS_MIX_MASK, (sizeof(int) + sizeof(double2)) * nvec + sizeof(double2) * nblk * nvec + 64, &e);
   FAME_CK(e, "mixed workspace");
   double2* dot = (double2*)sc;
@@ -364,8 +379,8 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
   FAME_CK(e, "lanczos workspace");
   double2* ddot = (double2*)workspace(P, WS_LZ_DOT, sizeof(double2) * na * 2 * 64, &e);
   FAME_CK(e, "lanczos workspace");
-  const int nblk1 = dot_blocks(L, 1);
-  const int nblkb = dot_blocks(L, na);
+  const int nblk1 = dot_blocks(P, L, 1);
+  const int nblkb = dot_blocks(P, L, na);
   double2* part = (double2*)workspace(P, WS_LZ_PART, sizeof(double2) * std::max(nblk1 * 64, nblkb * na) + 64, &e);
   FAME_CK(e, "lanczos workspace");
   FAME_CK(ensure_work(P, na), "lanczos scratch");
@@ -763,7 +778,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         FAME_CK(h2d_async(P, al2, ones.data(), sizeof(double2) * k0), "lz res");
         FAME_CK(h2d_async(P, al2 + k0, mw.data(), sizeof(double2) * k0), "lz res");
         FAME_CK(axpby_batched<double>(BX, AX, L, L, k0, al2, al2 + k0, nullptr, st), "lz res");
-        const int nb = dot_blocks(L, k0);
+        const int nb = dot_blocks(P, L, k0);
         double2* pp = (double2*)workspace(P, WS_LZ_INST + 54, sizeof(double2) * (nb * k0 + 2 * k0) + 64, &e);
         FAME_CK(e, "lz res");
         double2* o1 = pp + (size_t)nb * k0;

@@ -452,11 +452,13 @@ def profile_cg(nvec):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=8, help="k-points per step (batched band solve)")
+    ap.add_argument("--batch", type=int, default=10,
+                    help="k-points per step (batched band solve); 10 = the 40-point path in four steps, whose "
+                         "fncB runs as two sub-batches of 5 vectors (fills the last wave of plane-kernel CTAs)")
     ap.add_argument("--impl", choices=["fame", "reference"], default="fame")
-    ap.add_argument("--e2e-steps", type=int, default=5,
+    ap.add_argument("--e2e-steps", type=int, default=4,
                     help="end-to-end steps (capped at --steps; the same batches as the timed steps)")
     ap.add_argument("--fp64-kpoints", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

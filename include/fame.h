@@ -92,7 +92,8 @@ int fame_set_option(fame_plan_t plan, int option, double value);
 /*
  * Autotuner (no reference counterpart): time the launch parameters of the
  * fncB sequence for precision `prec` and batch width `nvec` on this plan
- * (vectors per launch sequence: the whole batch or 1/2, 1/4, 1/8 of it;
+ * (vectors per launch sequence: the whole batch, 1/2, 1/4, 1/8 of it or any
+ * width up to 16;
  * threads per block of the stencil kernels: 128, 256, 512) and keep the
  * fastest for later calls with that width.  Outputs (may be NULL): the chosen
  * chunk (0 = whole batch), block size and the measured microseconds of one
