@@ -410,9 +410,10 @@ def run_reference(args):
     }), flush=True)
 
 
-def profile_fncb(nvec, prec):
+def profile_fncb(nvec, prec, tune=None):
     """Three fncB applications to `nvec` vectors at n=60 (first `nvec` path
-    k-points): the workload of the committed ncu kernel captures."""
+    k-points): the workload of the committed ncu kernel captures.  `tune`
+    (chunk, stencil threads per block) installs fixed launch parameters."""
     import torch
 
     import fame
@@ -420,6 +421,8 @@ def profile_fncb(nvec, prec):
     torch.cuda.set_device(0)
     path = fame.band_path(npts=PATH_POINTS)
     plan = fame.woodpile_plan(N_GRID, path[np.arange(nvec) % len(path)])
+    if tune is not None:
+        plan.set_tune(prec, nvec, tune[0], tune[1])
     dt = torch.complex64 if prec == "c64" else torch.complex128
     x = torch.randn(nvec, 4 * N_GRID ** 3, dtype=dt, device="cuda")
     for _ in range(3):
@@ -466,11 +469,14 @@ def main():
     ap.add_argument("--profile-fncb", type=int, default=0, metavar="NVEC",
                     help="only apply fncB three times to NVEC vectors (for ncu captures) and exit")
     ap.add_argument("--profile-prec", choices=["c64", "c128"], default="c64")
+    ap.add_argument("--profile-tune", default=None, metavar="CHUNK,TPB",
+                    help="with --profile-fncb: vectors per launch sequence and stencil threads per block")
     ap.add_argument("--profile-cg", type=int, default=0, metavar="NVEC",
                     help="only run two 4-iteration complex64 CG solves on NVEC vectors (for ncu) and exit")
     args = ap.parse_args()
     if args.profile_fncb > 0:
-        profile_fncb(args.profile_fncb, args.profile_prec)
+        profile_fncb(args.profile_fncb, args.profile_prec,
+                     tuple(int(v) for v in args.profile_tune.split(",")) if args.profile_tune else None)
         return
     if args.profile_cg > 0:
         profile_cg(args.profile_cg)
