@@ -332,7 +332,8 @@ def run_fame(args):
                            fncb_tune={"chunk": int(tune["chunk"]), "stencil_tpb": int(tune["stencil_tpb"])},
                            precision="complex64 fncB + preconditioned CG, FP64 recurrence/reorth/residual "
                                      f"refinement (B^-1 to {INNER_TOL_MIXED:g}, tighter near Gamma)/NFSEP check",
-                           l2="inputs larger than L2 (Lanczos basis and B*Q of a batch ~5.3 GB)"),
+                           l2="inputs larger than L2 (Lanczos basis and B*Q of a batch "
+                              f"{2 * args.batch * LANCZOS_P_MIXED * 4 * N_GRID ** 3 * 16 / 1e9:.1f} GB)"),
             "e2e": {"value": None if e2e_value is None else round(e2e_value, 5), "unit": UNIT,
                     "h2d_bytes_per_step": int(h2d / max(1, e2e_steps)),
                     "d2h_bytes_per_step": int(d2h / max(1, e2e_steps)), "steps": e2e_steps,
