@@ -198,12 +198,15 @@ int fame_rasterize(int n, const double* lattice, int shape, const double* params
 
   const size_t Nq = (size_t)n * n * n;
   const bool host = (flags & FAME_HOST_PTR) != 0;
-  uint8_t* d = phase;
+  uint8_t* dbuf = nullptr;  // device staging of a host array
   cudaError_t e = cudaSuccess;
   if (host) {
-    e = cudaMalloc(&d, Nq);
-    if (e == cudaSuccess && g.paint) e = cudaMemcpy(d, phase, Nq, cudaMemcpyHostToDevice);
+    void* tmp = nullptr;
+    e = cudaMalloc(&tmp, Nq);
+    if (e == cudaSuccess) dbuf = (uint8_t*)tmp;
+    if (e == cudaSuccess && g.paint) e = cudaMemcpy(dbuf, phase, Nq, cudaMemcpyHostToDevice);
   }
+  uint8_t* d = host ? dbuf : phase;
   if (e == cudaSuccess) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -217,7 +220,7 @@ int fame_rasterize(int n, const double* lattice, int shape, const double* params
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = host ? cudaMemcpy(phase, d, Nq, cudaMemcpyDeviceToHost) : cudaDeviceSynchronize();
-  if (host && d) cudaFree(d);
+  if (dbuf) cudaFree(dbuf);
   if (e != cudaSuccess) return fail(nullptr, FAME_ERR_CUDA, std::string("fame_rasterize: ") + cudaGetErrorString(e));
   return FAME_OK;
 }
