@@ -48,10 +48,12 @@ INNER_TOL_MIXED = 1e-11    # B^{-1} of the mixed form (complex64 CG + FP64 resid
                            # eigenvalues within 5e-10 of the FP64 form (reported per run).
 # Lanczos restart size of the mixed form.  The reference uses p = 2k
 # (Computational_settings_Lanczos.m:30), which the plain FP64 sample keeps.
-# Four more columns cut the restarts at the batches holding Gamma, whose two
-# shifted zero modes occupy part of the Krylov space, by half: +23 % over the
-# path at n = 60, residuals <= 4e-9 (p = 28: +29 %, residuals up to 7.4e-9).
-LANCZOS_P_MIXED = 2 * BANDS + 4
+# More columns cut the restarts at the batches holding Gamma, whose two
+# shifted zero modes occupy part of the Krylov space: 2k + 4 gave +23 % over
+# the path at n = 60 (residuals <= 4e-9), 2k + 6 another +3 % (residuals
+# <= 5.2e-9); 2k + 8 adds 1.4 % more with residuals up to 7.4e-9, too close
+# to the 1e-8 bar.
+LANCZOS_P_MIXED = 2 * BANDS + 6
 RES_TOL = 1e-8
 PATH_POINTS = 40
 # B applies (fncB) of one plain-FP64 Lanczos band solve at n = 60 on this path
@@ -188,18 +190,21 @@ def run_fame(args):
     plans = {b: fame.woodpile_plan(N_GRID, batches[b]) for b in needed}
     # fncB launch parameters timed once on one plan (fame_autotune) and
     # installed on every plan of the run (fame_set_tune)
+    # (complex64 for the inner CG, complex128 for the FP64 residual refinement)
     tune = plans[needed[0]].autotune(nvec=args.batch, prec="c64")
+    tune128 = plans[needed[0]].autotune(nvec=args.batch, prec="c128")
 
     def set_tune(pl):
-        rc = lib.fame_set_tune(pl.raw, 1, args.batch, int(tune["chunk"]), int(tune["stencil_tpb"]))
-        if rc != 0:
-            raise RuntimeError("fame_set_tune failed")
+        for pr, t in ((1, tune), (0, tune128)):
+            rc = lib.fame_set_tune(pl.raw, pr, args.batch, int(t["chunk"]), int(t["stencil_tpb"]))
+            if rc != 0:
+                raise RuntimeError("fame_set_tune failed")
 
     for pl in plans.values():
         set_tune(pl)
 
     def solve(plan):
-        return plan.band_solve(BANDS, tol=LANCZOS_TOL, prec="c64", inner_tol=INNER_TOL_MIXED, p=LANCZOS_P_MIXED)
+        return plan.band_solve(BANDS, tol=LANCZOS_TOL, prec="c64", inner_tol=INNER_TOL_MIXED, p=args.lanczos_p)
 
     for s in range(args.warmup):
         solve(plans[bidx(s)])
@@ -255,7 +260,7 @@ def run_fame(args):
         th = np.stack([fame.bloch_angles(k, A) for k in kv])
         with fame.Plan(N_GRID, th, phase_host, tens) as pl:
             set_tune(pl)
-            r = pl.band_solve(BANDS, tol=LANCZOS_TOL, prec="c64", inner_tol=INNER_TOL_MIXED, p=LANCZOS_P_MIXED)
+            r = pl.band_solve(BANDS, tol=LANCZOS_TOL, prec="c64", inner_tol=INNER_TOL_MIXED, p=args.lanczos_p)
         h2d += phase_host.nbytes + th.nbytes + tens.nbytes * len(kv)
         d2h += r["ew"].nbytes + r["res"].nbytes + r["stats"].nbytes
     torch.cuda.synchronize()
@@ -307,7 +312,7 @@ def run_fame(args):
                     ew_mixed = r["ew"][:args.fp64_kpoints]
             if ew_mixed is None:
                 pm = fame.woodpile_plan(N_GRID, kv)
-                ew_mixed = pm.band_solve(BANDS, tol=LANCZOS_TOL, prec="c64", inner_tol=INNER_TOL_MIXED, p=LANCZOS_P_MIXED)["ew"]
+                ew_mixed = pm.band_solve(BANDS, tol=LANCZOS_TOL, prec="c64", inner_tol=INNER_TOL_MIXED, p=args.lanczos_p)["ew"]
                 pm.close()
             err = float(np.max(np.abs(ew_mixed - r64["ew"]) / np.abs(r64["ew"])))
             v64 = args.fp64_kpoints / t64
@@ -327,13 +332,14 @@ def run_fame(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "c64/f64", "data": "synthetic (woodpile geometry, "
             "band path generated in-run)",
             "config": dict(workload_config(args.batch),
-                           lanczos_p=LANCZOS_P_MIXED,
+                           lanczos_p=args.lanczos_p,
                            batching="consecutive path points, the two Gamma points in one batch",
                            fncb_tune={"chunk": int(tune["chunk"]), "stencil_tpb": int(tune["stencil_tpb"])},
+                           fncb_tune_c128={"chunk": int(tune128["chunk"]), "stencil_tpb": int(tune128["stencil_tpb"])},
                            precision="complex64 fncB + preconditioned CG, FP64 recurrence/reorth/residual "
                                      f"refinement (B^-1 to {INNER_TOL_MIXED:g}, tighter near Gamma)/NFSEP check",
                            l2="inputs larger than L2 (Lanczos basis and B*Q of a batch "
-                              f"{2 * args.batch * LANCZOS_P_MIXED * 4 * N_GRID ** 3 * 16 / 1e9:.1f} GB)"),
+                              f"{2 * args.batch * args.lanczos_p * 4 * N_GRID ** 3 * 16 / 1e9:.1f} GB)"),
             "e2e": {"value": None if e2e_value is None else round(e2e_value, 5), "unit": UNIT,
                     "h2d_bytes_per_step": int(h2d / max(1, e2e_steps)),
                     "d2h_bytes_per_step": int(d2h / max(1, e2e_steps)), "steps": e2e_steps,
@@ -462,6 +468,8 @@ def main():
                     help="k-points per step (batched band solve); 10 = the 40-point path in four steps, whose "
                          "fncB runs as two sub-batches of 5 vectors (fills the last wave of plane-kernel CTAs)")
     ap.add_argument("--impl", choices=["fame", "reference"], default="fame")
+    ap.add_argument("--lanczos-p", type=int, default=LANCZOS_P_MIXED,
+                    help="Lanczos restart size of the mixed form (the reference's p = 2k is kept by the FP64 form)")
     ap.add_argument("--e2e-steps", type=int, default=4,
                     help="end-to-end steps (capped at --steps; the same batches as the timed steps)")
     ap.add_argument("--fp64-kpoints", type=int, default=1)
