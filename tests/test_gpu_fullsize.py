@@ -88,3 +88,43 @@ def test_fncinvB_inverts_fncB(plan):
     x = plan.apply_Binv(b, tol=1e-10, maxit=10000, raise_on_noconv=True)
     x = x[0] if isinstance(x, tuple) else x
     assert rel(plan.apply_B(x), b) < 5e-10
+
+
+def test_empty_and_bad_batches(plan):
+    """An empty batch is a no-op; a negative count, missing vectors and an
+    instance index outside the plan are rejected before any device work."""
+    from fame import _lib as L
+
+    lib = fame.load()
+    h = plan.raw
+    for fn in (lib.fame_apply_A, lib.fame_apply_B):
+        assert fn(h, L.FAME_C128, None, None, 0, None, 0) == L.FAME_OK
+        assert fn(h, L.FAME_C128, None, None, -1, None, 0) == L.FAME_ERR_BAD_ARG
+        assert fn(h, L.FAME_C128, None, None, 1, None, 0) == L.FAME_ERR_BAD_ARG
+    assert lib.fame_apply_Binv(h, L.FAME_C128, None, None, 0, None, 1e-10, 100, None, None, 0) == L.FAME_OK
+    x = rand(4 * N ** 3, 1, 8)
+    y = torch.empty_like(x)
+    import ctypes as C
+
+    bad = (C.c_int * 1)(5)
+    rc = lib.fame_apply_B(h, L.FAME_C128, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), 1, bad, 0)
+    assert rc == L.FAME_ERR_BAD_ARG
+    assert b"instance" in lib.fame_last_error(h)
+
+
+def test_largest_compiled_grid(cuda, fame_lib):
+    """n = 64, the largest compiled size: DFT round trip, Hermitian fncB and
+    complex64 against complex128."""
+    n = 64
+    p = fame.woodpile_plan(n, [fame.fcc_point("W")])
+    try:
+        x3 = rand(3 * n ** 3, 1, 9)
+        assert rel(p.transform(p.transform(x3, 0), 1), x3) < 1e-13
+        x = rand(4 * n ** 3, 1, 10)
+        y = rand(4 * n ** 3, 1, 11)
+        bx, by = p.apply_B(x), p.apply_B(y)
+        s1, s2 = torch.vdot(y[0], bx[0]), torch.vdot(x[0], by[0]).conj()
+        assert abs(complex(s1 - s2)) < 1e-12 * float(torch.linalg.norm(y[0]) * torch.linalg.norm(bx[0]))
+        assert rel(p.apply_B(x.to(torch.complex64)).to(torch.complex128), bx) < 5e-5
+    finally:
+        p.close()
