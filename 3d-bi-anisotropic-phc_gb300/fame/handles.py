@@ -8,7 +8,6 @@ import math
 
 import numpy as np
 
-from . import _lib as L
 from .plan import Plan
 from .setup import bi_isotropic, bloch_angles, fcc_lattice, rasterize
 

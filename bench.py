@@ -20,7 +20,6 @@ from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -242,7 +241,6 @@ def run_fame(args):
     cgits = np.concatenate([r["stats"][:, 3] for r in results])
 
     # ---- end to end through the C ABI with host buffers -------------------
-    import fame.handles as H
 
     e2e_steps = max(0, min(args.steps, args.e2e_steps))
     A = fame.fcc_lattice()

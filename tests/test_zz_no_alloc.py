@@ -6,7 +6,6 @@ scratch.  Checked through the C ABI against fame_apply_B on two calls in a
 row (the array keeps the previous call's contents between them)."""
 import ctypes as C
 
-import numpy as np
 import pytest
 
 import fame
