@@ -521,10 +521,11 @@ int fame_apply_Binv(fame_plan_t h, int prec, const void* x, void* y, int nvec, c
 }
 
 int fame_material_blocks(const double* c6, const double* lattice, double* out) {
-  if (!c6 || !lattice || !out) return FAME_ERR_BAD_ARG;
+  if (!c6 || !lattice || !out) return fail(nullptr, FAME_ERR_BAD_ARG, "fame_material_blocks: null pointer");
   std::complex<double> M[36], Inv[36];
   for (int i = 0; i < 36; ++i) M[i] = std::complex<double>(c6[2 * i], c6[2 * i + 1]);
-  if (!invert_complex(M, Inv, 6)) return FAME_ERR_SINGULAR;
+  if (!invert_complex(M, Inv, 6))
+    return fail(nullptr, FAME_ERR_SINGULAR, "fame_material_blocks: singular constitutive block");
   // A: columns = primitive vectors; X_cov = A^T X A (Physical_settings_woodpile.m:184-194)
   const int off[3][2] = {{0, 0}, {3, 3}, {0, 3}};  // (1,1)=eps^-1 part -> N, (2,2) -> M, (1,2) -> J
   for (int b = 0; b < 3; ++b)
