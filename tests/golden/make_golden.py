@@ -7,7 +7,8 @@ reproduces them and `tests/test_gpu_golden.py` checks the CUDA library
 against them.  Inputs are deterministic closed-form vectors (no random
 generator whose stream could change between NumPy versions).
 
-    python tests/golden/make_golden.py      # rewrites woodpile_golden.npz
+    python tests/golden/make_golden.py          # rewrites woodpile_golden.npz
+    python tests/golden/make_golden.py --n24    # rewrites woodpile_n24_X.npz (~3 min)
 """
 from __future__ import annotations
 
@@ -24,6 +25,7 @@ if ROOT not in sys.path:
 import oracle as O  # noqa: E402
 
 FILE = os.path.join(HERE, "woodpile_golden.npz")
+N24_FILE = os.path.join(HERE, "woodpile_n24_X.npz")  # the first workload: n = 24, X point, 10 bands
 CASES = [(4, "X"), (6, "X"), (6, "L")]   # operator fixtures
 EIG_CASES = [(6, "X"), (6, "L")]          # Lanczos fixtures: k = 4, p = 8, tol 1e-10
 BANDS = 4
@@ -83,6 +85,20 @@ def compute():
     return out
 
 
+def compute_n24(k=10):
+    """The woodpile at n = 24 and the X point, the 10 largest eigenvalues of
+    B^-1 A by the oracle's Lanczos.m (p = 2k, tol 1e-10, inner pcg 1e-12)."""
+    P = O.build_problem(24, wave_vec=O.fcc_vertex("X"))
+    L = 4 * 24 ** 3
+    _, ew, it = O.lanczos(P.A, P.B, lambda r: O.fncinvB(r, P.B, 1e-12, 10000), L, k, 1e-10, 10000, 2 * k,
+                          np.ones(L, complex))
+    return {"ew": np.asarray(ew, dtype=np.float64), "theta": np.asarray(P.thetas, dtype=np.float64)}
+
+
 if __name__ == "__main__":
-    np.savez_compressed(FILE, **compute())
-    print("wrote", FILE, os.path.getsize(FILE), "bytes")
+    if "--n24" in sys.argv:
+        np.savez_compressed(N24_FILE, **compute_n24())
+        print("wrote", N24_FILE, os.path.getsize(N24_FILE), "bytes")
+    else:
+        np.savez_compressed(FILE, **compute())
+        print("wrote", FILE, os.path.getsize(FILE), "bytes")

@@ -40,6 +40,17 @@ def test_oracle_reproduces_fixtures(fresh):
             assert relerr(got, ref) < 1e-12, (key, relerr(got, ref))
 
 
+def test_first_workload_fixture():
+    """woodpile_n24_X.npz (written by make_golden.py --n24; ~3 minutes of
+    oracle time, so not recomputed here): 10 descending eigenvalues of
+    B^-1 A at the X point's Bloch angles."""
+    import oracle as O
+
+    f = np.load(G.N24_FILE)
+    assert f["ew"].shape == (10,) and np.all(np.diff(f["ew"]) < 0)
+    assert np.allclose(f["theta"], O.thetas_from_k(O.fcc_vertex("X")), rtol=1e-15, atol=0)
+
+
 def test_fixture_geometry_is_nontrivial():
     for name in ("raster_woodpile", "raster_sphere", "raster_tetra"):
         bits = np.unpackbits(FIX[name])[:G.RASTER_N ** 3]

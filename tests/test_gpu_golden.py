@@ -59,3 +59,18 @@ def test_rasteriser_matches_fixture(cuda, fame_lib):
     for n_, lab in G.CASES:
         got = fame.rasterize(n_, "woodpile", 0.25)
         assert np.array_equal(got, FIX[f"n{n_}_{lab}_inside"])
+
+
+def test_first_workload_n24_matches_fixture(cuda, fame_lib):
+    """The woodpile at n = 24, X point, 10 bands (the reference's own
+    CPU-sized case): the FP64 form equals the oracle's Lanczos.m
+    (tests/golden/woodpile_n24_X.npz) to 1e-10, the mixed form to 1e-8."""
+    ref = np.load(G.N24_FILE)["ew"]
+    plan = fame.woodpile_plan(24, [fame.fcc_point("X")])
+    r = plan.lanczos(10, tol=1e-10, maxit=10000, p=20, prec="c128", want_vectors=False)
+    assert r["status"] == 0
+    assert np.allclose(r["ew"], ref, rtol=1e-10, atol=0), (r["ew"], ref)
+    m = plan.band_solve(10, tol=1e-10, prec="c64", inner_tol=1e-11, p=26)
+    assert m["status"] == 0
+    assert np.allclose(m["ew"][0], ref, rtol=1e-8, atol=0), (m["ew"][0], ref)
+    assert m["res"].max() <= 1e-8
