@@ -230,8 +230,10 @@ def rasterize(n: int, shape: str, size: float, A: np.ndarray | None = None, cent
     tetrahedron include their 27 periodic images.  Returns a uint8 numpy array,
     or a CUDA uint8 tensor when `device` (or when `phase` is one)."""
     A = fcc_lattice() if A is None else A
-    lib = load()
+    if shape not in SHAPES:
+        raise ValueError(f"unknown shape {shape!r}: one of {sorted(SHAPES)}")
     kind = SHAPES[shape]
+    lib = load()
     if kind == 0:
         params = np.array([size, a], dtype=np.float64)
     else:

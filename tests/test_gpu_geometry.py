@@ -121,3 +121,7 @@ def test_bad_arguments_rejected_on_host(fame_lib):
         assert b"fame_rasterize" in fame_lib.fame_last_error(None)
     with pytest.raises(fame.FameError):
         fame.rasterize(2, "woodpile", -1.0)
+    with pytest.raises(ValueError, match="unknown shape"):
+        fame.rasterize(2, "cube", 0.25)
+    with pytest.raises(ValueError, match="n\\^3"):
+        fame.rasterize(2, "woodpile", 0.25, phase=np.zeros(5, dtype=np.uint8))
