@@ -5,7 +5,8 @@
 //                any width up to 16): smaller sub-batches keep the six-field
 //                intermediates in L2, and some widths fill the last wave of
 //                CTAs better than others;
-//   stencil_tpb  threads per block of the two stencil kernels (128/256/512).
+//   stencil_tpb  the material stencil's form: 0 the single-pass k_sweep,
+//                128/256/512 threads per block of the two-kernel form.
 // No counterpart in the reference.
 #include <algorithm>
 #include <vector>
@@ -20,6 +21,9 @@ TuneEntry tune_for(const Plan& P, int prec, int nvec) {
   TuneEntry d;
   d.prec = prec;
   d.nvec = nvec;
+  // complex64: single pass (two CTAs per SM); complex128 stages twice the
+  // bytes per plane and keeps the two-kernel form unless tuned otherwise
+  d.stencil_tpb = prec == FAME_C64 ? 0 : 256;
   return d;
 }
 
@@ -66,7 +70,7 @@ static int autotune_prec(Plan& P, int nvec, int reps, TuneEntry* best_out) {
   TuneEntry best;
   best.us = 1e300;
   for (int c : chunks)
-    for (int tpb : {128, 256, 512}) {
+    for (int tpb : {0, 128, 256, 512}) {
       TuneEntry t;
       t.prec = prec;
       t.nvec = nvec;
@@ -123,7 +127,7 @@ int fame_autotune(fame_plan_t h, int prec, int nvec, int* chunk, int* stencil_tp
 int fame_set_tune(fame_plan_t h, int prec, int nvec, int chunk, int stencil_tpb) {
   if (!h) return FAME_ERR_BAD_ARG;
   Plan& P = h->P;
-  if (nvec < 1 || chunk < 0 || (stencil_tpb != 128 && stencil_tpb != 256 && stencil_tpb != 512) ||
+  if (nvec < 1 || chunk < 0 || (stencil_tpb != 0 && stencil_tpb != 128 && stencil_tpb != 256 && stencil_tpb != 512) ||
       (prec != FAME_C64 && prec != FAME_C128))
     return fail(&P, FAME_ERR_BAD_ARG, "fame_set_tune: bad argument");
   TuneEntry t;

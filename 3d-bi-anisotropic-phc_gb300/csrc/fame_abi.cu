@@ -339,6 +339,20 @@ int fame_set_option(fame_plan_t h, int option, double value) {
     case FAME_OPT_GRAPH:
       P.opt_graph = value != 0.0;
       return FAME_OK;
+    case FAME_OPT_SIRA_NEAREST:
+      P.opt_sira_nearest = value != 0.0;
+      return FAME_OK;
+    case FAME_OPT_REFINE:
+      P.opt_refine = value != 0.0;
+      return FAME_OK;
+    case FAME_OPT_REFINE_TOL:
+      if (!(value > 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: refine tol in (0, 1)");
+      P.opt_refine_tol = value;
+      return FAME_OK;
+    case FAME_OPT_PLANE_SPLIT:
+      P.opt_plane_split = value != 0.0;
+      free_graphs(P);  // captured sequences hold the old kernels
+      return FAME_OK;
     case FAME_OPT_ITOL_FLOOR:
       if (!(value > 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: itol floor in (0, 1)");
       P.opt_itol_floor = value;
@@ -362,6 +376,14 @@ int fame_sync(fame_plan_t h) {
   if (!h) return FAME_ERR_BAD_ARG;
   cudaError_t e = cudaStreamSynchronize(h->P.stream);
   return e == cudaSuccess ? FAME_OK : cuda_fail(&h->P, e, "fame_sync");
+}
+
+int fame_refine_residuals(fame_plan_t h, double* before, int n) {
+  if (!h) return fail(nullptr, FAME_ERR_BAD_ARG, "fame_refine_residuals: null plan");
+  const std::vector<double>& r = h->P.refine_res_before;
+  if (before)
+    for (int i = 0; i < n && i < (int)r.size(); ++i) before[i] = r[i];
+  return (int)r.size();
 }
 
 const char* fame_last_error(fame_plan_t h) { return h ? h->P.last_error.c_str() : g_static_error.c_str(); }

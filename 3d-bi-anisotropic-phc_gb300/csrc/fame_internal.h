@@ -38,12 +38,12 @@ inline VecCtx sub_ctx(const VecCtx& c, int v0) {
 }
 
 // Launch parameters of the fncB sequence picked by fame_autotune for one
-// (precision, batch width): vectors per launch sequence and threads per block
-// of the stencil kernels.
+// (precision, batch width): vectors per launch sequence and the material
+// stencil's form (single pass, or threads per block of the two-kernel form).
 struct TuneEntry {
   int prec = 0, nvec = 0;
   int chunk = 0;         // 0: whole batch
-  int stencil_tpb = 256;
+  int stencil_tpb = 0;   // 0: single-pass k_sweep; 128/256/512: two-kernel form
   double us = 0.0;       // measured time of one fncB on the batch
 };
 
@@ -82,6 +82,11 @@ struct Plan {
   double opt_tol32 = 1e-6;            // complex64 CG tolerance of the first refinement round
   int opt_graph = 1;                  // replay CG iterations from captured CUDA graphs
   double opt_itol_floor = 1e-13;      // mixed form: floor of the spread-scaled inner tolerance
+  int opt_plane_split = 1;            // fncB plane kernels with several threads per pencil where compiled
+  int opt_sira_nearest = 0;           // SIRA Ritz choice: 0 'CL' (above the target), 1 nearest either side
+  int opt_refine = 1;                 // mixed form: FP64 refinement sweep of the Ritz pairs
+  double opt_refine_tol = 1e-12;      // its inner B^{-1} tolerance
+  std::vector<double> refine_res_before;  // NFSEP residuals before the last refinement sweep
   std::vector<double> theta;          // [nk][3]
   std::vector<double> sigma_min;      // [nk] smallest curl singular value sqrt(min |L|^2)
   std::vector<double> mat_avg;        // [nk][27][2] volume-averaged Herm(N) | Herm(M) | J
@@ -142,9 +147,12 @@ int fail(Plan* P, int code, const std::string& msg);
 int cuda_fail(Plan* P, cudaError_t e, const char* where);
 
 // ---- kernel launchers (fncb_kernels.cu) ----
+// pq (may be null): partial sums of Re(x^H B x), fncB_pq_partials(P, nvec)
+// per vector, written when that count is non-zero.
 template <class R>
 cudaError_t launch_fncB(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,
-                        cx<R>* w0, cx<R>* w1, cudaStream_t st);
+                        cx<R>* w0, cx<R>* w1, cudaStream_t st, double2* pq = nullptr);
+template <class R> int fncB_pq_partials(const Plan& P, int nvec);
 template <class R>
 cudaError_t launch_fncA(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,
                         cudaStream_t st);

@@ -26,8 +26,9 @@
 // Pipeline (one launch each):
 //   plane_inv  : Pi blocks per frequency voxel + inverse DFT along x and y
 //   col        : inverse DFT along z (in place)
-//   vertex     : U, V, Hu, Hv at every vertex (fncb_material.cuh)
-//   faceedge   : u', v' (in place over u, v)
+//   sweep      : u', v' in one pass into the second buffer (fncb_material.cuh),
+//                or the two-kernel form: vertex (U, V, Hu, Hv at every vertex
+//                into scratch) then faceedge (u', v' in place)
 //   col        : forward DFT along z
 //   plane_fwd  : forward DFT along y and x + Pi^H blocks
 //
@@ -268,6 +269,255 @@ k_plane_fwd(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, V
 }
 
 // ---------------------------------------------------------------------------
+// Split-pencil plane kernels of fncB (k_plane_inv2 / k_plane_fwd2): the same
+// work as k_plane_inv<PREP> / k_plane_fwd<POST>, with G threads per pencil
+// instead of one.  A length N = G*M with gcd(G, M) = 1 is split by the
+// prime-factor index map (no twiddle factors):
+//   n = (M*n1 + G*n2) mod N,  k = (M*A*k1 + G*B*k2) mod N,
+//   A = M^{-1} mod G, B = G^{-1} mod M,
+//   X[k] = sum_{n2} W_M^{n2 k2} sum_{n1} x[n] W_G^{n1 k1}.
+// Pass A: M length-G DFTs over n1 per pencil, in place in shared memory
+// (thread g of the pencil takes n2 = g, g+G, ...).  Pass B: thread k1 takes
+// the length-M DFT over n2 in registers.  A thread then holds M complex
+// values instead of N, so 3*N*G threads of a CTA fit two CTAs per SM
+// (N = 60: G = 3, 540 threads, 34 warps per SM against 12 for one thread per
+// 60-point pencil).
+// ---------------------------------------------------------------------------
+FAME_HD constexpr int plane_split(int n) {
+  return n == 60 ? 3 : n == 48 ? 3 : n == 40 ? 5 : n == 36 ? 4 : n == 30 ? 3 : n == 24 ? 3 : n == 20 ? 4
+       : n == 12 ? 3 : 0;
+}
+
+template <int N, int G> struct Split {
+  static constexpr int M = N / G;
+  static constexpr int A = fft_inv_mod(M % G, G);
+  static constexpr int B = fft_inv_mod(G % M, M);
+  static constexpr int T = 3 * N * G;                 // threads: (field, pencil, g)
+  static constexpr int TB = ((T + 31) / 32) * 32;
+  static constexpr int NA = (M + G - 1) / G;          // pass-A DFTs per thread (upper bound)
+  static_assert(G * M == N && A >= 0 && B >= 0, "coprime split");
+  FAME_HD static constexpr int in_slot(int n1, int n2) { return (M * n1 + G * n2) % N; }
+  FAME_HD static constexpr int out_slot(int k1, int k2) { return (M * A * k1 + G * B * k2) % N; }
+};
+
+// Pass A on one pencil in shared memory (element i at p[i * STRIDE]) for the
+// thread with sub-pencil index GC (compile time, so that every slot index is
+// an immediate offset).
+template <class R, int N, int G, int S, int STRIDE, int GC>
+__device__ __forceinline__ void split_pass_a(cx<R>* p) {
+  using SP = Split<N, G>;
+  static_for<0, SP::NA>([&](auto jc) {
+    constexpr int n2 = GC + decltype(jc)::value * G;
+    if constexpr (n2 < SP::M) {
+      cx<R> a[G];
+      static_for<0, G>([&](auto n1c) { a[decltype(n1c)::value] = p[SP::in_slot(decltype(n1c)::value, n2) * STRIDE]; });
+      fft<R, G, S>(a);
+      static_for<0, G>([&](auto n1c) { p[SP::in_slot(decltype(n1c)::value, n2) * STRIDE] = a[decltype(n1c)::value]; });
+    }
+  });
+}
+
+// Pass B read: the M values of row K1 of one pencil.
+template <class R, int N, int G, int STRIDE, int K1>
+__device__ __forceinline__ void split_pass_b_load(const cx<R>* p, cx<R> (&z)[N / G]) {
+  using SP = Split<N, G>;
+  static_for<0, SP::M>([&](auto n2c) { z[decltype(n2c)::value] = p[SP::in_slot(K1, decltype(n2c)::value) * STRIDE]; });
+}
+
+// Pass B write: X[out_slot(K1, k2)] = z[k2].
+template <class R, int N, int G, int STRIDE, int K1, class P>
+__device__ __forceinline__ void split_pass_b_store(P p, const cx<R> (&z)[N / G]) {
+  using SP = Split<N, G>;
+  static_for<0, SP::M>([&](auto k2c) { p[(long long)SP::out_slot(K1, decltype(k2c)::value) * STRIDE] = z[decltype(k2c)::value]; });
+}
+
+// f(integral_constant<GC>) for the runtime g of this thread (warps are
+// uniform in g except the ones that straddle two sub-pencil groups).
+template <int G, class F> __device__ __forceinline__ void with_g(int g, F&& f) {
+  static_for<0, G>([&](auto gc) {
+    if (g == decltype(gc)::value) f(gc);
+  });
+}
+
+template <class R, int N, bool PREP_UNUSED = true>
+__global__ void __launch_bounds__(Split<N, plane_split(N)>::TB, sizeof(R) == 4 ? 2 : 1)
+k_plane_inv2(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d, VecCtx ctx,
+             long long in_stride, long long in_side_stride, long long out_stride, int side0) {
+  constexpr int G = plane_split(N);
+  using SP = Split<N, G>;
+  constexpr int M = SP::M, T = SP::T, LD = N + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);  // [3][N][LD]
+  const int k3 = blockIdx.x;
+  const int vec = blockIdx.z;
+  if (ctx.active && !ctx.active[vec]) return;
+  const int inst = vec_inst(ctx, vec);
+  const int side = side0 + blockIdx.y;
+  const long long Nq = (long long)N * N * N;
+  const cx<R>* lam = d.lam + (long long)inst * 3 * N;
+  const cx<R>* xin = x + vec * in_stride + blockIdx.y * in_side_stride + (long long)k3 * N * N;
+  const int tid = threadIdx.x;
+  // Pi blocks (frequency voxel -> 3 components of this side), scaled by 1/n
+  // for the two inverse DFTs; all loads of a thread issued together.
+  {
+    constexpr int ITEMS = (N * N + T - 1) / T;
+    cx<R> in[ITEMS][2];
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it) {
+      const int e = tid + it * T;
+      if (tid < T && e < N * N) {
+        in[it][0] = xin[e];
+        in[it][1] = xin[Nq + e];
+      }
+    }
+    const R sc = R(1) / R(N);
+    const cx<R> lz = lam[2 * N + k3];
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it) {
+      const int e = tid + it * T;
+      if (tid < T && e < N * N) {
+        const int i2 = e / N, i1 = e - i2 * N;
+        PiBlock<R> P = pi_block<R>(lam[i1], lam[N + i2], lz);
+        const cx<R> a = cscale(in[it][0], sc), b = cscale(in[it][1], sc);
+        cx<R> v0, v1, v2;
+        if (side == 0) {
+          v0 = cfmac(P.p1[0], b, cneg(cmulc(P.p2[0], a)));
+          v1 = cfmac(P.p1[1], b, cneg(cmulc(P.p2[1], a)));
+          v2 = cfmac(P.p1[2], b, cneg(cmulc(P.p2[2], a)));
+        } else {
+          v0 = cfma(P.p2[0], b, cmul(P.p1[0], a));
+          v1 = cfma(P.p2[1], b, cmul(P.p1[1], a));
+          v2 = cfma(P.p2[2], b, cmul(P.p1[2], a));
+        }
+        sm[(0 * N + i2) * LD + i1] = v0;
+        sm[(1 * N + i2) * LD + i1] = v1;
+        sm[(2 * N + i2) * LD + i1] = v2;
+      }
+    }
+  }
+  __syncthreads();
+  const int g = tid / (3 * N);
+  const int cp = tid - g * (3 * N);
+  const int c = cp / N, p = cp - c * N;
+  const bool act = tid < T;
+  // x rows (pencil p = row i2 of field c)
+  if (act) with_g<G>(g, [&](auto gc) { split_pass_a<R, N, G, +1, 1, decltype(gc)::value>(sm + (c * N + p) * LD); });
+  __syncthreads();
+  {
+    cx<R> z[M];
+    if (act)
+      with_g<G>(g, [&](auto gc) { split_pass_b_load<R, N, G, 1, decltype(gc)::value>(sm + (c * N + p) * LD, z); });
+    if (act) fft<R, M, +1>(z);
+    __syncthreads();
+    if (act)
+      with_g<G>(g, [&](auto gc) { split_pass_b_store<R, N, G, 1, decltype(gc)::value>(sm + (c * N + p) * LD, z); });
+  }
+  __syncthreads();
+  // y columns (pencil p = column i1 of field c), written straight to global
+  if (act) with_g<G>(g, [&](auto gc) { split_pass_a<R, N, G, +1, LD, decltype(gc)::value>(sm + c * N * LD + p); });
+  __syncthreads();
+  if (act) {
+    cx<R> z[M];
+    with_g<G>(g, [&](auto gc) { split_pass_b_load<R, N, G, LD, decltype(gc)::value>(sm + c * N * LD + p, z); });
+    fft<R, M, +1>(z);
+    cx<R>* o = out + vec * out_stride + (long long)(blockIdx.y * 3 + c) * Nq + (long long)k3 * N * N + p;
+    with_g<G>(g, [&](auto gc) { split_pass_b_store<R, N, G, N, decltype(gc)::value>(o, z); });
+  }
+}
+
+template <class R, int N, bool POST_UNUSED = true>
+__global__ void __launch_bounds__(Split<N, plane_split(N)>::TB, sizeof(R) == 4 ? 2 : 1)
+k_plane_fwd2(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, VecCtx ctx,
+             long long w_stride, long long out_stride, long long out_side_stride, int side0) {
+  constexpr int G = plane_split(N);
+  using SP = Split<N, G>;
+  constexpr int M = SP::M, T = SP::T, LD = N + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);  // [3][N][LD]
+  const int k3 = blockIdx.x;
+  const int vec = blockIdx.z;
+  if (ctx.active && !ctx.active[vec]) return;
+  const int inst = vec_inst(ctx, vec);
+  const int side = side0 + blockIdx.y;
+  const long long Nq = (long long)N * N * N;
+  const int tid = threadIdx.x;
+  const int g = tid / (3 * N);
+  const int cp = tid - g * (3 * N);
+  const int c = cp / N, p = cp - c * N;
+  const bool act = tid < T;
+  // y columns, pass A straight from global (pencil p = column i1 of field c)
+  if (act) {
+    const cx<R>* src = w + vec * w_stride + (long long)(blockIdx.y * 3 + c) * Nq + (long long)k3 * N * N + p;
+    cx<R>* col = sm + c * N * LD + p;
+    with_g<G>(g, [&](auto gc) {
+      constexpr int GC = decltype(gc)::value;
+      cx<R> a[SP::NA][G];
+      static_for<0, SP::NA>([&](auto jc) {
+        constexpr int n2 = GC + decltype(jc)::value * G;
+        if constexpr (n2 < M)
+          static_for<0, G>([&](auto n1c) {
+            a[decltype(jc)::value][decltype(n1c)::value] = src[(long long)SP::in_slot(decltype(n1c)::value, n2) * N];
+          });
+      });
+      static_for<0, SP::NA>([&](auto jc) {
+        constexpr int j = decltype(jc)::value;
+        constexpr int n2 = GC + j * G;
+        if constexpr (n2 < M) {
+          fft<R, G, -1>(a[j]);
+          static_for<0, G>([&](auto n1c) { col[SP::in_slot(decltype(n1c)::value, n2) * LD] = a[j][decltype(n1c)::value]; });
+        }
+      });
+    });
+  }
+  __syncthreads();
+  {
+    cx<R> z[M];
+    if (act)
+      with_g<G>(g, [&](auto gc) { split_pass_b_load<R, N, G, LD, decltype(gc)::value>(sm + c * N * LD + p, z); });
+    if (act) fft<R, M, -1>(z);
+    __syncthreads();
+    if (act)
+      with_g<G>(g, [&](auto gc) { split_pass_b_store<R, N, G, LD, decltype(gc)::value>(sm + c * N * LD + p, z); });
+  }
+  __syncthreads();
+  // x rows (pencil p = row i2 of field c)
+  if (act) with_g<G>(g, [&](auto gc) { split_pass_a<R, N, G, -1, 1, decltype(gc)::value>(sm + (c * N + p) * LD); });
+  __syncthreads();
+  {
+    cx<R> z[M];
+    if (act)
+      with_g<G>(g, [&](auto gc) { split_pass_b_load<R, N, G, 1, decltype(gc)::value>(sm + (c * N + p) * LD, z); });
+    if (act) fft<R, M, -1>(z);
+    __syncthreads();
+    if (act)
+      with_g<G>(g, [&](auto gc) { split_pass_b_store<R, N, G, 1, decltype(gc)::value>(sm + (c * N + p) * LD, z); });
+  }
+  __syncthreads();
+  // Pi^H blocks of this side, scaled by 1/n for the two forward DFTs
+  const cx<R>* lam = d.lam + (long long)inst * 3 * N;
+  cx<R>* o = y + vec * out_stride + blockIdx.y * out_side_stride + (long long)k3 * N * N;
+  const cx<R> lz = lam[2 * N + k3];
+  const R sc = R(1) / R(N);
+  for (int e = tid; e < N * N; e += SP::TB) {
+    const int i2 = e / N, i1 = e - i2 * N;
+    const cx<R> u0 = sm[(0 * N + i2) * LD + i1];
+    const cx<R> u1 = sm[(1 * N + i2) * LD + i1];
+    const cx<R> u2 = sm[(2 * N + i2) * LD + i1];
+    PiBlock<R> P = pi_block<R>(lam[i1], lam[N + i2], lz);
+    cx<R> a, b;
+    if (side == 0) {
+      a = cneg(cfma(P.p2[2], u2, cfma(P.p2[1], u1, cmul(P.p2[0], u0))));
+      b = cfma(P.p1[2], u2, cfma(P.p1[1], u1, cmul(P.p1[0], u0)));
+    } else {
+      a = cfmac(P.p1[2], u2, cfmac(P.p1[1], u1, cmulc(P.p1[0], u0)));
+      b = cfmac(P.p2[2], u2, cfmac(P.p2[1], u1, cmulc(P.p2[0], u0)));
+    }
+    o[e] = cscale(a, sc);
+    o[Nq + e] = cscale(b, sc);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // col: DFT along z of every (i1, i2) column, in place; one thread per column.
 // SMODE 1: multiply S_z(i3) after (inverse); 2: multiply conj(S_z(i3)) before
 // (forward).  Scale 1/sqrt(n).
@@ -307,8 +557,19 @@ template <class R, int N, bool PREP, bool WITH_S>
 cudaError_t plane_inv(const Plan& P, const PlanData<R>& d, const cx<R>* x, cx<R>* out, int nvec,
                       int nside, int side0, long long in_stride, long long in_side_stride,
                       long long out_stride, const VecCtx& ctx, cudaStream_t st) {
-  const int threads = ((3 * N + 31) / 32) * 32;
   const size_t sm = sizeof(cx<R>) * 3 * N * (N + 1);
+  if constexpr (PREP && !WITH_S && plane_split(N) > 0) {
+    if (P.opt_plane_split) {
+      auto kfn = k_plane_inv2<R, N>;
+      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return e;
+      FAME_LAUNCHED(1);
+      kfn<<<dim3(N, nside, nvec), Split<N, plane_split(N)>::TB, sm, st>>>(x, out, d, ctx, in_stride, in_side_stride,
+                                                                           out_stride, side0);
+      return cudaGetLastError();
+    }
+  }
+  const int threads = ((3 * N + 31) / 32) * 32;
   auto kfn = k_plane_inv<R, N, PREP, WITH_S>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
@@ -322,8 +583,19 @@ template <class R, int N, bool POST, bool WITH_S>
 cudaError_t plane_fwd(const Plan& P, const PlanData<R>& d, const cx<R>* w, cx<R>* y, int nvec, int nside,
                       int side0, long long w_stride, long long out_stride, long long out_side_stride,
                       const VecCtx& ctx, cudaStream_t st) {
-  const int threads = ((3 * N + 31) / 32) * 32;
   const size_t sm = sizeof(cx<R>) * 3 * N * (N + 1);
+  if constexpr (POST && !WITH_S && plane_split(N) > 0) {
+    if (P.opt_plane_split) {
+      auto kfn = k_plane_fwd2<R, N>;
+      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return e;
+      FAME_LAUNCHED(1);
+      kfn<<<dim3(N, nside, nvec), Split<N, plane_split(N)>::TB, sm, st>>>(w, y, d, ctx, w_stride, out_stride,
+                                                                           out_side_stride, side0);
+      return cudaGetLastError();
+    }
+  }
+  const int threads = ((3 * N + 31) / 32) * 32;
   auto kfn = k_plane_fwd<R, N, POST, WITH_S>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
@@ -346,9 +618,15 @@ cudaError_t col(const PlanData<R>& d, cx<R>* w, int nfield, int nvec, long long 
 // fncB on a batch, as sub-batches of `chunk` vectors (0: all at once) so that
 // the six-field intermediates of a sub-batch can stay in L2; the stencil
 // kernels run with tpb threads per block.  Both come from fame_autotune.
+//
+// pq (may be null): with the single-pass stencil, per-CTA partial sums of
+// Re(x^H B x) (sweep_partials per vector, vector-major).  The curl-SVD
+// transforms are unitary and Pi has orthonormal columns, so x^H B x equals
+// w^H [M J^H; J N] w for the spatial fields w the stencil reads; the stencil
+// pass accumulates it while it writes its output.
 template <class R, int N>
 cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx, cx<R>* w0, cx<R>* w1,
-                   cudaStream_t st) {
+                   cudaStream_t st, double2* pq) {
   const PlanData<R>& d = pdata<R>(P);
   const long long Nq = P.Nq;
   const TuneEntry tn = tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec);
@@ -363,11 +641,18 @@ cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecC
     if (e != cudaSuccess) return e;
     e = col<R, N, +1, 0>(d, w0, 6, nv, 6 * Nq, c, st);
     if (e != cudaSuccess) return e;
-    e = stencil_n<R, N>(P, w0, w1, nv, c, st, tn.stencil_tpb);
+    // material stencil: single pass w0 -> w1, or the two-kernel form in place on w0
+    cx<R>* wm = w0;
+    if (tn.stencil_tpb == 0) {
+      e = sweep_n<R, N>(P, w0, w1, nv, c, st, pq ? pq + (size_t)v0 * sweep_partials_n<R, N>() : nullptr);
+      wm = w1;
+    } else {
+      e = stencil_n<R, N>(P, w0, w1, nv, c, st, tn.stencil_tpb);
+    }
     if (e != cudaSuccess) return e;
-    e = col<R, N, -1, 0>(d, w0, 6, nv, 6 * Nq, c, st);
+    e = col<R, N, -1, 0>(d, wm, 6, nv, 6 * Nq, c, st);
     if (e != cudaSuccess) return e;
-    e = plane_fwd<R, N, true, false>(P, d, w0, ys, nv, 2, 0, 6 * Nq, 4 * Nq, 2 * Nq, c, st);
+    e = plane_fwd<R, N, true, false>(P, d, wm, ys, nv, 2, 0, 6 * Nq, 4 * Nq, 2 * Nq, c, st);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -431,7 +716,7 @@ cudaError_t handle_n(const Plan& P, int which, const cx<R>* x, cx<R>* y, int nve
 // suppress instantiation in other translation units).
 #define FAME_SIZE_SIGS(PFX, R, NN)                                                                                 \
   PFX cudaError_t fame::detail::fncB_n<R, NN>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&, cx<R>*,       \
-                                              cx<R>*, cudaStream_t);                                               \
+                                              cx<R>*, cudaStream_t, double2*);                                     \
   PFX cudaError_t fame::detail::stencil_n<R, NN>(const Plan&, cx<R>*, cx<R>*, int, const VecCtx&, cudaStream_t,    \
                                                  int);                                                             \
   PFX cudaError_t fame::detail::fields_inv_n<R, NN>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&,         \

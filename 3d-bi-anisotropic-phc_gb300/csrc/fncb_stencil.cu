@@ -77,6 +77,19 @@ template cudaError_t stencil<double>(const Plan&, cx<double>*, cx<double>*, int,
 }  // namespace detail
 using namespace detail;
 
+// Partials per vector that fncB's pq output receives for a batch of nvec, or
+// 0 when the tuned form of that batch does not produce them.
+template <class R>
+int fncB_pq_partials(const Plan& P, int nvec) {
+  if (tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).stencil_tpb != 0) return 0;
+  switch (P.n) {
+#define FAME_CASE(NN) case NN: return sweep_partials_n<R, NN>();
+    FAME_FOR_EACH_N(FAME_CASE)
+#undef FAME_CASE
+    default: return 0;
+  }
+}
+
 bool n_supported(int n) {
   switch (n) {
 #define FAME_CASE(NN) case NN: return NN >= 2;
@@ -88,10 +101,10 @@ bool n_supported(int n) {
 
 template <class R>
 cudaError_t launch_fncB(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx, cx<R>* w0,
-                        cx<R>* w1, cudaStream_t st) {
+                        cx<R>* w1, cudaStream_t st, double2* pq) {
   if (nvec <= 0) return cudaSuccess;
   switch (P.n) {
-#define FAME_CASE(NN) case NN: return fncB_n<R, NN>(P, x, y, nvec, ctx, w0, w1, st);
+#define FAME_CASE(NN) case NN: return fncB_n<R, NN>(P, x, y, nvec, ctx, w0, w1, st, pq);
     FAME_FOR_EACH_N(FAME_CASE)
 #undef FAME_CASE
     default: return cudaErrorInvalidValue;
@@ -171,7 +184,8 @@ cudaError_t launch_material(const Plan& P, const cx<R>* uv, cx<R>* out, int nvec
 
 #define FAME_INST(R)                                                                                      \
   template cudaError_t launch_fncB<R>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&, cx<R>*,     \
-                                      cx<R>*, cudaStream_t);                                              \
+                                      cx<R>*, cudaStream_t, double2*);                                    \
+  template int fncB_pq_partials<R>(const Plan&, int);                                                     \
   template cudaError_t launch_fncA<R>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&,             \
                                       cudaStream_t);                                                      \
   template cudaError_t launch_fields_inv<R>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&,       \

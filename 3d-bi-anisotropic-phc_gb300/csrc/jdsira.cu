@@ -3,7 +3,8 @@
 //
 // The reference calls Driver4(fncB, fncA, ...), so its pencil is
 //   fncB x = theta fncA x      (theta = omega, the frequency)
-// and it targets the Ritz values closest to `target` ('CL').  Per outer step:
+// and it targets the Ritz values closest to `target` from above ('CL'; the
+// option FAME_OPT_SIRA_NEAREST takes the closest on either side).  Per outer step:
 //   * projected pencil  V^H B V y = theta V^H A V y  on the Euclidean-orthonormal
 //     search space V, which also holds the locked eigenvectors (Locking4.m:91-103,115)
 //   * the Ritz pair closest to the target among the unlocked ones (the locked
@@ -508,6 +509,15 @@ int jdsira_run(Plan& P, int inst, int inner_prec, int nev, double target, double
     std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return wlock[a] > wlock[b]; });
     std::vector<int> cand(idx.begin() + std::min(nl, m), idx.end());
     auto theta_of = [&](int c2) { return mu[c2] != 0.0 ? 1.0 / mu[c2] : 1e300; };
+    if (!P.opt_sira_nearest) {
+      // 'CL' of Choose_Ritz_Pair_Unsymm4.m:176-186,218-224: the Ritz values
+      // above the target, closest first; all of them by distance only when
+      // none lies above
+      std::vector<int> above;
+      for (int c2 : cand)
+        if (theta_of(c2) > target) above.push_back(c2);
+      if (!above.empty()) cand.swap(above);
+    }
     std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) {
       return std::fabs(theta_of(a) - target) < std::fabs(theta_of(b) - target);
     });

@@ -28,6 +28,20 @@ cudaError_t cg_p(cx<R>* p, const cx<R>* r, long long len, long long stride, int 
                  const int* active, cudaStream_t st);
 cudaError_t cg_scalars(int stage, int nvec, const double2* dot, double* rho, double* alpha, double* beta,
                        const double* tol2b2, int* active, int* iters, double* res2, cudaStream_t st);
+// cg_scalars on the sums of nblk partials per vector (partial[v * nblk + i]),
+// the sums also stored in dot[v]; one launch.
+cudaError_t cg_scalars_red(int stage, int nvec, const double2* partial, int nblk, double2* dot, double* rho,
+                           double* alpha, double* beta, const double* tol2b2, int* active, int* iters, double* res2,
+                           cudaStream_t st);
+// partial[v * nblk + i] = block i's share of a_v^H b_v (no final reduction)
+template <class R>
+cudaError_t dot_partial(const cx<R>* a, const cx<R>* b, long long len, long long stride, int nvec, double2* partial,
+                        int nblk, const int* active, cudaStream_t st);
+// x += alpha p ; r -= alpha q ; partial (|r|^2, |r|^2) per block (no final reduction)
+template <class R>
+cudaError_t cg_xr_partial(cx<R>* x, cx<R>* r, const cx<R>* p, const cx<R>* q, long long len, long long stride,
+                          int nvec, const double* alpha, const int* active, double2* partial, int nblk,
+                          cudaStream_t st);
 template <class R>
 cudaError_t block_rot(const cx<R>* in, cx<R>* out, long long len, long long ld, int p, int k, const double* U,
                       cudaStream_t st);
@@ -68,8 +82,11 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
 
 // Mixed-precision B^{-1}: complex64 CG corrections inside FP64 residual
 // refinement until ||b - B x|| <= tol ||b|| (FP64).  Bx receives B*x (FP64).
+// cg_vec / b64_vec (host, may be null): per-vector complex64 CG iterations and
+// FP64 B applies, added to.
 int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, const int* d_inst, double tol,
                   int max_rounds, double inner_tol32, int maxit32, const unsigned char* h_mask,
-                  long long* cg_iters, long long* b64_applies, const double* tol_per_vec = nullptr);
+                  long long* cg_iters, long long* b64_applies, const double* tol_per_vec = nullptr,
+                  long long* cg_vec = nullptr, long long* b64_vec = nullptr);
 
 }  // namespace fame

@@ -211,6 +211,51 @@ __global__ void k_cg_scalars(int stage, int nvec, const double2* __restrict__ do
   }
 }
 
+// k_cg_scalars preceded by the reduction of the vector's nblk partials (one
+// CTA per vector; the block sum has a fixed order, so the iterates repeat
+// run to run).
+__global__ void __launch_bounds__(kRedThreads)
+k_cg_scalars_red(int stage, const double2* __restrict__ partial, int nblk, double2* __restrict__ dot,
+                 double* __restrict__ rho, double* __restrict__ alpha, double* __restrict__ beta,
+                 const double* __restrict__ tol2b2, int* __restrict__ active, int* __restrict__ iters,
+                 double* __restrict__ res2) {
+  const int v = blockIdx.x;
+  if (!active[v]) return;
+  double2 s = make_double2(0.0, 0.0);
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
+    const double2 p = partial[(long long)v * nblk + i];
+    s.x += p.x;
+    s.y += p.y;
+  }
+  s = block_sum2(s);
+  if (threadIdx.x != 0) return;
+  dot[v] = s;
+  const int it = iters[v] + 1;
+  if (stage == 0) {
+    const double pq = s.x;
+    alpha[v] = (pq != 0.0 && isfinite(pq)) ? rho[v] / pq : 0.0;
+    if (!(pq > 0.0) || !isfinite(pq)) {  // breakdown: B must be HPD
+      active[v] = 0;
+      iters[v] = -it;
+    }
+  } else {
+    const double rz = s.x, rn = s.y;  // (Re r'z, |r|^2), z = M r (z = r without preconditioner)
+    res2[v] = rn;
+    beta[v] = rho[v] != 0.0 ? rz / rho[v] : 0.0;
+    rho[v] = rz;
+    iters[v] = it;
+    if (!isfinite(rn) || !isfinite(rz)) {
+      active[v] = 0;
+      iters[v] = -it;
+    } else if (rn <= tol2b2[v]) {
+      active[v] = 0;
+    } else if (!(rz > 0.0)) {
+      active[v] = 0;
+      iters[v] = -it;
+    }
+  }
+}
+
 // out[:, j] = sum_i in[:, i] * U[i, j]  (U real, p x k, column-major), all columns of one vector block
 template <class R>
 __global__ void k_block_rot(const cx<R>* __restrict__ in, cx<R>* __restrict__ out, long long len,
@@ -397,6 +442,33 @@ cudaError_t cg_xr_dot(cx<R>* x, cx<R>* r, const cx<R>* p, const cx<R>* q, long l
 }
 
 template <class R>
+cudaError_t dot_partial(const cx<R>* a, const cx<R>* b, long long len, long long stride, int nvec, double2* partial,
+                        int nblk, const int* active, cudaStream_t st) {
+  if (nvec <= 0) return cudaSuccess;
+  FAME_LAUNCHED(1);
+  k_dot_partial<R><<<dim3(nblk, nvec, 1), kRedThreads, 0, st>>>(a, stride, 0, 1, b, stride, len, partial, active);
+  return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t cg_xr_partial(cx<R>* x, cx<R>* r, const cx<R>* p, const cx<R>* q, long long len, long long stride,
+                          int nvec, const double* alpha, const int* active, double2* partial, int nblk,
+                          cudaStream_t st) {
+  FAME_LAUNCHED(1);
+  k_cg_xr_dot<R><<<dim3(nblk, nvec), kRedThreads, 0, st>>>(x, r, p, q, len, stride, alpha, active, partial);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_scalars_red(int stage, int nvec, const double2* partial, int nblk, double2* dot, double* rho,
+                           double* alpha, double* beta, const double* tol2b2, int* active, int* iters, double* res2,
+                           cudaStream_t st) {
+  FAME_LAUNCHED(1);
+  k_cg_scalars_red<<<nvec, kRedThreads, 0, st>>>(stage, partial, nblk, dot, rho, alpha, beta, tol2b2, active, iters,
+                                                 res2);
+  return cudaGetLastError();
+}
+
+template <class R>
 cudaError_t cg_p(cx<R>* p, const cx<R>* r, long long len, long long stride, int nvec, const double* beta,
                  const int* active, cudaStream_t st) {
   int gx = grid_for(len);
@@ -511,7 +583,11 @@ template cudaError_t scale_batched<float>(const cx<float>*, cx<float>*, long lon
   template cudaError_t block_rot<R>(const cx<R>*, cx<R>*, long long, long long, int, int, const double*, \
                                     cudaStream_t);                                                        \
   template cudaError_t sub_combo<R>(cx<R>*, const cx<R>*, long long, long long, int, const double2*,     \
-                                    cudaStream_t);
+                                    cudaStream_t);                                                        \
+  template cudaError_t dot_partial<R>(const cx<R>*, const cx<R>*, long long, long long, int, double2*,   \
+                                      int, const int*, cudaStream_t);                                     \
+  template cudaError_t cg_xr_partial<R>(cx<R>*, cx<R>*, const cx<R>*, const cx<R>*, long long, long long, \
+                                        int, const double*, const int*, double2*, int, cudaStream_t);
 FAME_KINST(float)
 FAME_KINST(double)
 template cudaError_t convert<float, double>(const cx<double>*, cx<float>*, long long, cudaStream_t);

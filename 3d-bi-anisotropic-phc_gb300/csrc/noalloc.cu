@@ -14,7 +14,8 @@
 // exits.  In host code the array's name is only a host-side stand-in, so the
 // device address is looked up with cudaGetSymbolAddress once per device (with
 // that device current) on the first call on that device; make that first call
-// before any stream capture.  The call allocates nothing: no cudaMalloc, no
+// before any stream capture.  The plan's device must be the current device
+// when the entry point is called (it is checked).  The call allocates nothing: no cudaMalloc, no
 // cudaFree, no allocating library routine.  All calls share the one array and
 // it keeps the last call's contents; the fncB pipeline overwrites both scratch
 // fields before reading them, so nothing needs clearing, but calls whose
@@ -58,8 +59,17 @@ cudaError_t scratch_address(void** out) {
 using namespace fame;
 
 extern "C" int fame_apply_B_noalloc(fame_plan_t h, int prec, const void* x, void* y, int nvec) {
-  if (!h) return FAME_ERR_BAD_ARG;
+  if (!h) return fail(nullptr, FAME_ERR_BAD_ARG, "fame_apply_B_noalloc: null plan");
   Plan& P = h->P;
+  // The scratch address is per device and looked up on the current one, so
+  // the plan's device must be current (the library never switches devices).
+  int cur = -1;
+  cudaError_t de = cudaGetDevice(&cur);
+  if (de != cudaSuccess) return cuda_fail(&P, de, "fame_apply_B_noalloc device");
+  if (cur != P.device)
+    return fail(&P, FAME_ERR_BAD_ARG,
+                "fame_apply_B_noalloc: the plan's device " + std::to_string(P.device) + " is not current (device " +
+                    std::to_string(cur) + " is)");
   if (prec != FAME_C128 && prec != FAME_C64) return fail(&P, FAME_ERR_BAD_ARG, "fame_apply_B_noalloc: bad precision");
   if (nvec < 0 || (nvec > 0 && (!x || !y))) return fail(&P, FAME_ERR_BAD_ARG, "fame_apply_B_noalloc: bad vectors");
   if (nvec == 0) return FAME_OK;

@@ -21,7 +21,9 @@ enum WsId {
   WS_PCG_R = 0, WS_PCG_P, WS_PCG_Q, WS_PCG_SCAL, WS_PCG_PART,
   WS_MIX_B32, WS_MIX_X32, WS_MIX_RES, WS_MIX_MASK, WS_MIX_BD, WS_PCG_Z,
   WS_LZ_Q, WS_LZ_BQ, WS_LZ_VEC, WS_LZ_TMP, WS_LZ_COEF, WS_LZ_INST, WS_LZ_MASK, WS_LZ_U, WS_LZ_SCAL, WS_LZ_DOT,
-  WS_LZ_PART
+  WS_LZ_PART,
+  WS_RF_X = 200, WS_RF_AX, WS_RF_BX, WS_RF_Y, WS_RF_BY, WS_RF_AY, WS_RF_R, WS_RF_Z, WS_RF_INST, WS_RF_G, WS_RF_C,
+  WS_RF_PART
 };
 
 #define FAME_CK(expr, where)                      \
@@ -87,7 +89,11 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
   S.active = (int*)(S.res2 + nvec);
   S.iters = S.active + nvec;
   const int nblk = dot_blocks(P, L, nvec);
-  double2* part = (double2*)workspace(P, WS_PCG_PART, sizeof(double2) * nblk * nvec + 64, &e);
+  // p^H B p from the stencil pass of fncB where its tuned form provides it
+  const int nblk_pq = fncB_pq_partials<R>(P, nvec);
+  const int nblkv0 = dot_blocks(P, P.Nq, nvec);
+  const int npart = std::max(std::max(nblk, nblk_pq), nblkv0);
+  double2* part = (double2*)workspace(P, WS_PCG_PART, sizeof(double2) * npart * nvec + 64, &e);
   FAME_CK(e, "pcg workspace");
   FAME_CK(ensure_work(P, nvec), "pcg fncB scratch");
   cx<R>* w0 = (cx<R>*)P.d_work;
@@ -150,19 +156,25 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
   // One CG iteration: every kernel reads its scalars and active flags from
   // the device, so a block of iterations is a fixed launch sequence that is
   // captured once per (sizes, pointers) and replayed from a CUDA graph.
+  //   q = B p (with the partials of p^H q when the stencil pass provides them)
+  //   alpha = rho / p^H q            (partials reduced in the same launch)
+  //   x += alpha p, r -= alpha q, z = M r, partials of (r^H z, |r|^2)
+  //   beta, rho, convergence         (partials reduced in the same launch)
+  //   p = z + beta p
   auto iteration = [&](cudaStream_t cs) -> cudaError_t {
-    cudaError_t e2 = launch_fncB<R>(P, p, q, nvec, ctx, w0, w1, cs);
-    if (e2 == cudaSuccess) e2 = dot_batched<R>(p, L, 0, 1, q, L, L, nvec, S.dot, part, nblk, S.active, cs);
+    cudaError_t e2 = launch_fncB<R>(P, p, q, nvec, ctx, w0, w1, cs, nblk_pq ? part : nullptr);
+    if (e2 == cudaSuccess && !nblk_pq) e2 = dot_partial<R>(p, q, L, L, nvec, part, nblk, S.active, cs);
     if (e2 == cudaSuccess)
-      e2 = cg_scalars(0, nvec, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active, S.iters, S.res2, cs);
+      e2 = cg_scalars_red(0, nvec, part, nblk_pq ? nblk_pq : nblk, S.dot, S.rho, S.alpha, S.beta, S.tol2b2,
+                          S.active, S.iters, S.res2, cs);
     if (pre) {
       if (e2 == cudaSuccess) e2 = pcg_update<R>(P, x, r, z, p, q, nvec, ctx, S.alpha, part, nblkv, cs);
-      if (e2 == cudaSuccess) e2 = dot_final(part, nblkv, nvec, S.dot, cs);
     } else if (e2 == cudaSuccess) {
-      e2 = cg_xr_dot<R>(x, r, p, q, L, L, nvec, S.alpha, S.active, S.dot, part, nblk, cs);
+      e2 = cg_xr_partial<R>(x, r, p, q, L, L, nvec, S.alpha, S.active, part, nblk, cs);
     }
     if (e2 == cudaSuccess)
-      e2 = cg_scalars(1, nvec, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active, S.iters, S.res2, cs);
+      e2 = cg_scalars_red(1, nvec, part, pre ? nblkv : nblk, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active,
+                          S.iters, S.res2, cs);
     if (e2 == cudaSuccess) e2 = cg_p<R>(p, pre ? z : r, L, L, nvec, S.beta, S.active, cs);
     return e2;
   };
@@ -173,7 +185,8 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
                                        (uintptr_t)d_inst, (uintptr_t)nblk, (uintptr_t)nblkv,
                                        sizeof(R) == 4 ? (uintptr_t)P.d32.pc : (uintptr_t)P.d64.pc,
                                        (uintptr_t)tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).chunk,
-                                       (uintptr_t)tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).stencil_tpb};
+                                       (uintptr_t)tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).stencil_tpb,
+                                       (uintptr_t)nblk_pq, (uintptr_t)P.opt_plane_split};
   bool use_graph = P.opt_graph != 0;
   bool any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
   for (int it = 1; it <= maxit && any; it += chk) {
@@ -223,7 +236,7 @@ template int pcg_batched<double>(Plan&, const double2*, double2*, int, const int
 
 int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, const int* d_inst, double tol,
                   int max_rounds, double inner_tol32, int maxit32, const unsigned char* h_mask, long long* cg_iters,
-                  long long* b64_applies, const double* tol_per_vec) {
+                  long long* b64_applies, const double* tol_per_vec, long long* cg_vec, long long* b64_vec) {
   if (nvec <= 0) return FAME_OK;
   auto tol_of = [&](int v) { return tol_per_vec ? tol_per_vec[v] : tol; };
   cudaStream_t st = P.stream;
@@ -287,15 +300,20 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
                                  tolv.data());
     if (prc == FAME_ERR_NAN || prc == FAME_ERR_BREAKDOWN) return prc;
     for (int v = 0; v < nvec; ++v)
-      if (m[v] && cg_iters) *cg_iters += std::abs(its[v]);
+      if (m[v]) {
+        if (cg_iters) *cg_iters += std::abs(its[v]);
+        if (cg_vec) cg_vec[v] += std::abs(its[v]);
+      }
     FAME_CK(refine_acc(x, d32, L, nvec, dmask, st), "mixed acc");
     if (round != 1) {
       // exact FP64 residual b - B x
       double2* w0 = (double2*)P.d_work;
       double2* w1 = w0 + (size_t)nvec * 6 * P.Nq;
       FAME_CK(launch_fncB<double>(P, x, Bx, nvec, ctx, w0, w1, st), "mixed fncB");
-      if (b64_applies)
-        for (int v = 0; v < nvec; ++v) *b64_applies += m[v];
+      for (int v = 0; v < nvec; ++v) {
+        if (b64_applies) *b64_applies += m[v];
+        if (b64_vec) b64_vec[v] += m[v];
+      }
     } else {
       // B x = (B x_prev) + B d with B d in complex64: d is already ~1e-6 of x,
       // so its complex64 apply adds ~1e-13 relative error to B x.
@@ -320,6 +338,168 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
   }
   if (std::any_of(m.begin(), m.end(), [](unsigned char a) { return a != 0; })) rc = FAME_ERR_NOT_CONVERGED;
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 refinement sweep of converged Ritz pairs (no reference counterpart:
+// the reference's FP64 Lanczos needs none).  For the k Ritz vectors X of
+// every instance, batched over all instances:
+//   Y = B^{-1} A X               mixed-precision inner solve to `tol`
+//   [X Y]^H A [X Y] c = lambda [X Y]^H B [X Y] c     FP64 Rayleigh-Ritz
+// (one step of block inverse iteration with Rayleigh-Ritz on the doubled
+// space), keeping the k largest lambda, as Lanczos.m:109 orders them.  The
+// NFSEP residual ||B x - omega A x|| (EvaluteError_Chiral_no_inv.m:20, x
+// B-normalised, omega = 1/lambda) is evaluated in FP64 before and after.
+// X: [na*k][4Nq] B-normalised Ritz vectors, overwritten by the refined ones;
+// lam: [na][k] in and out.
+// ---------------------------------------------------------------------------
+int ritz_refine(Plan& P, const std::vector<int>& insts, int k, double2* X, double* lam, double* res_before,
+                double* res_after, double tol, long long* b64_vec, long long* cg_vec) {
+  const int na = (int)insts.size();
+  if (na == 0 || k < 1) return FAME_OK;
+  cudaStream_t st = P.stream;
+  const long long L = 4 * P.Nq;
+  const int nv = na * k;
+  const size_t cb = sizeof(double2) * L;
+  cudaError_t e;
+  double2* AX = (double2*)workspace(P, WS_RF_AX, cb * nv, &e);
+  FAME_CK(e, "refine workspace");
+  double2* BX = (double2*)workspace(P, WS_RF_BX, cb * nv, &e);
+  FAME_CK(e, "refine workspace");
+  double2* Y = (double2*)workspace(P, WS_RF_Y, cb * nv, &e);
+  FAME_CK(e, "refine workspace");
+  double2* BY = (double2*)workspace(P, WS_RF_BY, cb * nv, &e);
+  FAME_CK(e, "refine workspace");
+  double2* AY = (double2*)workspace(P, WS_RF_AY, cb * nv, &e);
+  FAME_CK(e, "refine workspace");
+  double2* Z = (double2*)workspace(P, WS_RF_Z, cb * 2 * k, &e);
+  FAME_CK(e, "refine workspace");
+  int* dinst = (int*)workspace(P, WS_RF_INST, sizeof(int) * nv + 64, &e);
+  FAME_CK(e, "refine workspace");
+  const int ncall = 8 * k;  // (A, B) x (X rows, Y rows) x 2k columns
+  double2* G = (double2*)workspace(P, WS_RF_G, sizeof(double2) * ((size_t)ncall * na * k + 4 * nv) + 64, &e);
+  FAME_CK(e, "refine workspace");
+  double2* scal = G + (size_t)ncall * na * k;  // [2][nv] axpby scalars, [nv] norms
+  double2* C = (double2*)workspace(P, WS_RF_C, sizeof(double2) * (size_t)na * 2 * k * k + 64, &e);
+  FAME_CK(e, "refine workspace");
+  const int nblk = dot_blocks(P, L, std::max(na, nv));
+  double2* part = (double2*)workspace(P, WS_RF_PART, sizeof(double2) * (size_t)nblk * nv + 64, &e);
+  FAME_CK(e, "refine workspace");
+  FAME_CK(ensure_work(P, nv), "refine scratch");
+  std::vector<int> hi(nv);
+  for (int a = 0; a < na; ++a)
+    for (int i = 0; i < k; ++i) hi[(size_t)a * k + i] = insts[a];
+  FAME_CK(h2d_async(P, dinst, hi.data(), sizeof(int) * nv), "refine init");
+  VecCtx ctx;
+  ctx.inst = dinst;
+  ctx.nk = P.nk;
+  double2* W0 = (double2*)P.d_work;
+  double2* W1 = W0 + (size_t)nv * 6 * P.Nq;
+  // NFSEP residuals of (lam, V) with AV, BV given: R = BV - (1/lam) AV (into AY)
+  auto nfsep = [&](const double2* AV, const double2* BV, const double* lm, double* out) -> int {
+    std::vector<double2> ab(2 * (size_t)nv);
+    for (int i = 0; i < nv; ++i) {
+      ab[i] = make_double2(1.0, 0.0);
+      ab[nv + i] = make_double2(-1.0 / lm[i], 0.0);
+    }
+    FAME_CK(h2d_async(P, scal, ab.data(), sizeof(double2) * 2 * nv), "refine residual");
+    FAME_CK(cudaMemcpyAsync(AY, AV, cb * nv, cudaMemcpyDeviceToDevice, st), "refine residual");
+    FAME_CK(axpby_batched<double>(BV, AY, L, L, nv, scal, scal + nv, nullptr, st), "refine residual");
+    FAME_CK(dot_batched<double>(AY, L, 0, 1, AY, L, L, nv, scal + 2 * nv, part, nblk, nullptr, st), "refine residual");
+    std::vector<double2> h(nv);
+    FAME_CK(cudaMemcpyAsync(h.data(), scal + 2 * nv, sizeof(double2) * nv, cudaMemcpyDeviceToHost, st), "refine residual");
+    FAME_CK(cudaStreamSynchronize(st), "refine residual");
+    for (int i = 0; i < nv; ++i) out[i] = std::sqrt(std::max(0.0, h[i].x));
+    return FAME_OK;
+  };
+  // A X, B X and the residuals before
+  FAME_CK(launch_fncA<double>(P, X, AX, nv, ctx, st), "refine fncA");
+  FAME_CK(launch_fncB<double>(P, X, BX, nv, ctx, W0, W1, st), "refine fncB");
+  for (int i = 0; i < nv; ++i) b64_vec[i]++;
+  std::vector<double> rb(nv);
+  int rc = nfsep(AX, BX, lam, rb.data());
+  if (rc) return rc;
+  if (res_before) std::copy(rb.begin(), rb.end(), res_before);
+  // Y = B^{-1} A X (FP64-accurate mixed solve), A Y
+  long long cgi = 0, b64 = 0;
+  rc = solve_B_mixed(P, AX, Y, BY, nv, dinst, tol, 8, P.opt_tol32, 4000, nullptr, &cgi, &b64, nullptr, cg_vec,
+                     b64_vec);
+  if (rc == FAME_ERR_NAN || rc == FAME_ERR_BREAKDOWN) return rc;
+  FAME_CK(launch_fncA<double>(P, Y, AY, nv, ctx, st), "refine fncA");
+  // Gram matrices G_A = Z^H A Z, G_B = Z^H B Z per instance, Z = [X_a Y_a]:
+  // call c = ((op * 2 + rowblk) * 2k + col) fills G[c][a][0..k)
+  const long long vs = (long long)k * L;  // instance stride inside X, Y, AX, ...
+  for (int op = 0; op < 2; ++op)
+    for (int rb2 = 0; rb2 < 2; ++rb2)
+      for (int col = 0; col < 2 * k; ++col) {
+        const double2* rows = rb2 == 0 ? X : Y;
+        const double2* cv = op == 0 ? (col < k ? AX : AY) : (col < k ? BX : BY);
+        cv += (size_t)(col % k) * L;
+        const int c = (op * 2 + rb2) * 2 * k + col;
+        FAME_CK(dot_batched<double>(rows, vs, L, k, cv, vs, L, na, G + (size_t)c * na * k, part, nblk, nullptr, st),
+                "refine gram");
+      }
+  std::vector<double2> hG((size_t)ncall * na * k);
+  FAME_CK(cudaMemcpyAsync(hG.data(), G, sizeof(double2) * hG.size(), cudaMemcpyDeviceToHost, st), "refine gram");
+  FAME_CK(cudaStreamSynchronize(st), "refine gram");
+  const int m = 2 * k;
+  std::vector<double2> hC((size_t)na * m * k);
+  std::vector<double> lam_new((size_t)nv);
+  for (int a = 0; a < na; ++a) {
+    std::vector<std::complex<double>> GA((size_t)m * m), GB((size_t)m * m);
+    for (int op = 0; op < 2; ++op)
+      for (int rb2 = 0; rb2 < 2; ++rb2)
+        for (int col = 0; col < m; ++col) {
+          const int c = (op * 2 + rb2) * m + col;
+          for (int r = 0; r < k; ++r) {
+            const double2 v = hG[((size_t)c * na + a) * k + r];  // conj(row_r)^H . (Op z_col)
+            (op == 0 ? GA : GB)[(size_t)(rb2 * k + r) * m + col] = std::complex<double>(v.x, v.y);
+          }
+        }
+    for (int i = 0; i < m; ++i)  // Hermitian parts
+      for (int j = 0; j < i; ++j) {
+        const auto ga = 0.5 * (GA[(size_t)i * m + j] + std::conj(GA[(size_t)j * m + i]));
+        GA[(size_t)i * m + j] = ga;
+        GA[(size_t)j * m + i] = std::conj(ga);
+        const auto gb = 0.5 * (GB[(size_t)i * m + j] + std::conj(GB[(size_t)j * m + i]));
+        GB[(size_t)i * m + j] = gb;
+        GB[(size_t)j * m + i] = std::conj(gb);
+      }
+    for (int i = 0; i < m; ++i) {
+      GA[(size_t)i * m + i] = GA[(size_t)i * m + i].real();
+      GB[(size_t)i * m + i] = GB[(size_t)i * m + i].real();
+    }
+    std::vector<double> mu;
+    std::vector<std::complex<double>> Yv;
+    if (!herm_pencil_eig(GA, GB, m, mu, Yv)) return fail(&P, FAME_ERR_BREAKDOWN, "refine: [X Y]^H B [X Y] not definite");
+    std::vector<int> ind(m);
+    std::iota(ind.begin(), ind.end(), 0);
+    std::stable_sort(ind.begin(), ind.end(), [&](int x, int y) { return mu[x] > mu[y]; });
+    for (int j = 0; j < k; ++j) {
+      lam_new[(size_t)a * k + j] = mu[ind[j]];
+      for (int i = 0; i < m; ++i) {
+        const auto v = Yv[(size_t)ind[j] * m + i];
+        hC[((size_t)a * k + j) * m + i] = make_double2(v.real(), v.imag());  // column j of instance a (m x k)
+      }
+    }
+  }
+  FAME_CK(h2d_async(P, C, hC.data(), sizeof(double2) * hC.size()), "refine combine");
+  // X_a <- [X_a Y_a] C_a
+  for (int a = 0; a < na; ++a) {
+    FAME_CK(cudaMemcpyAsync(Z, X + (size_t)a * vs, cb * k, cudaMemcpyDeviceToDevice, st), "refine combine");
+    FAME_CK(cudaMemcpyAsync(Z + (size_t)k * L, Y + (size_t)a * vs, cb * k, cudaMemcpyDeviceToDevice, st),
+            "refine combine");
+    FAME_CK(block_comb<double>(Z, X + (size_t)a * vs, L, L, m, k, C + (size_t)a * m * k, st), "refine combine");
+  }
+  std::copy(lam_new.begin(), lam_new.end(), lam);
+  // residuals after
+  FAME_CK(launch_fncA<double>(P, X, AX, nv, ctx, st), "refine fncA");
+  FAME_CK(launch_fncB<double>(P, X, BX, nv, ctx, W0, W1, st), "refine fncB");
+  for (int i = 0; i < nv; ++i) b64_vec[i]++;
+  std::vector<double> ra(nv);
+  if ((rc = nfsep(AX, BX, lam, ra.data()))) return rc;
+  if (res_after) std::copy(ra.begin(), ra.end(), res_after);
+  return FAME_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -458,6 +638,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
       FAME_CK(h2d_async(P, V + (size_t)a * L, hv.data(), cb), "lanczos v0");
     FAME_CK(fncB64(V, BV), "lanczos v0");
     total_b += na;
+    for (int a = 0; a < na; ++a) S[a].bapplies++;
     std::vector<double2> vb;
     int rc = batched_dot(V, BV, vb);
     if (rc) return rc;
@@ -518,12 +699,16 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     if (mixed) {
       long long cgi = 0, b64 = 0;
       std::vector<double> tv(na);
+      std::vector<long long> cgv(na, 0), bv(na, 0);
       for (int a = 0; a < na; ++a) tv[a] = S[a].itol;
-      rc = solve_B_mixed(P, AQ, PR, BPR, na, dinst, itol, 8, P.opt_tol32, 2000, hm.data(), &cgi, &b64, tv.data());
+      rc = solve_B_mixed(P, AQ, PR, BPR, na, dinst, itol, 8, P.opt_tol32, 2000, hm.data(), &cgi, &b64, tv.data(),
+                         cgv.data(), bv.data());
       if (rc == FAME_ERR_NAN || rc == FAME_ERR_BREAKDOWN) return rc;
       total_b += b64;
-      for (int a = 0; a < na; ++a)
-        if (mask[a]) S[a].cgits += cgi / std::max(1, (int)std::count(mask.begin(), mask.end(), 1));
+      for (int a = 0; a < na; ++a) {
+        S[a].cgits += cgv[a];
+        S[a].bapplies += bv[a];
+      }
     } else {
       std::vector<int> its(na, 0);
       rc = pcg_batched<double>(P, AQ, PR, na, dinst, itol, 10000, its.data(), nullptr, hm.data());
@@ -531,6 +716,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
       for (int a = 0; a < na; ++a)
         if (mask[a]) {
           S[a].cgits += std::abs(its[a]);
+          S[a].bapplies += std::abs(its[a]);
           total_b += std::abs(its[a]);
         }
     }
@@ -585,7 +771,10 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     // rr = fncB(r); beta = sqrt(r'*rr); v = r/beta  (Lanczos.m:72-74)
     if (!mixed) {
       FAME_CK(fncB64(PR, BPR), "lanczos fncB");
-      for (int a = 0; a < na; ++a) total_b += mask[a];
+      for (int a = 0; a < na; ++a) {
+        total_b += mask[a];
+        S[a].bapplies += mask[a];
+      }
     } else {
       // Instances with an extreme Ritz-value spread (the shifted zero modes
       // near Gamma) take B r by an explicit FP64 apply, as Lanczos.m:72 does:
@@ -601,7 +790,10 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         FAME_CK(h2d_async(P, dmask, xm.data(), sizeof(int) * na), "lanczos mask");
         FAME_CK(fncB64(PR, BPR), "lanczos fncB");
         FAME_CK(upload_mask(), "lanczos mask");
-        for (int a = 0; a < na; ++a) total_b += xm[a];
+        for (int a = 0; a < na; ++a) {
+          total_b += xm[a];
+          S[a].bapplies += xm[a];
+        }
       }
     }
     std::vector<double2> rr;
@@ -707,6 +899,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         double2* w0 = (double2*)P.d_work;
         FAME_CK(launch_fncB<double>(P, Qa, BQa, k, ck, w0, w0 + (size_t)k * 6 * P.Nq, st), "lz restart");
         total_b += k;
+        I.bapplies += k;
         I.refresh_bq = false;
       }
       FAME_CK(cudaStreamSynchronize(st), "lz restart");
@@ -728,16 +921,40 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
   for (int a = 0; a < na; ++a) {
     LzInst& I = S[a];
     for (int i = 0; i < k0; ++i) ew[(size_t)a * k0 + i] = I.d[i];
-    if (stats) {
-      stats[a * 4 + 0] = I.steps;
-      stats[a * 4 + 1] = I.restarts;
-      stats[a * 4 + 2] = 0;
-      stats[a * 4 + 3] = I.cgits;
+  }
+  P.refine_res_before.clear();
+  if (mixed && P.opt_refine) {
+    // FP64 refinement sweep of every Ritz pair (ritz_refine), batched over the instances
+    double2* X = (double2*)workspace(P, WS_RF_X, cb * (size_t)na * k0, &e);
+    FAME_CK(e, "refine workspace");
+    for (int a = 0; a < na; ++a) {
+      LzInst& I = S[a];
+      const int np = (int)(I.U.size() / k0);
+      FAME_CK(h2d_async(P, dU, I.U.data(), sizeof(double) * I.U.size()), "lz ritz");
+      FAME_CK(block_rot<double>(Q + (size_t)a * p * L, X + (size_t)a * k0 * L, L, L, np, k0, dU, st), "lz ritz");
     }
+    std::vector<double> rb((size_t)na * k0), ra((size_t)na * k0);
+    std::vector<long long> bv((size_t)na * k0, 0), cv((size_t)na * k0, 0);
+    int rrc = ritz_refine(P, insts, k0, X, ew, rb.data(), ra.data(), P.opt_refine_tol, bv.data(), cv.data());
+    if (rrc != FAME_OK) return rrc;
+    for (int a = 0; a < na; ++a)
+      for (int i = 0; i < k0; ++i) {
+        S[a].bapplies += bv[(size_t)a * k0 + i];
+        S[a].cgits += cv[(size_t)a * k0 + i];
+      }
+    P.refine_res_before = rb;
+    if (EV) FAME_CK(cudaMemcpyAsync(EV, X, cb * (size_t)na * k0, cudaMemcpyDeviceToDevice, st), "refine out");
+    if (res) std::copy(ra.begin(), ra.end(), res);
+    FAME_CK(cudaStreamSynchronize(st), "refine out");
   }
   if (stats)
-    for (int a = 0; a < na; ++a) stats[a * 4 + 2] = total_b / na;
-  if (EV || res) {
+    for (int a = 0; a < na; ++a) {
+      stats[a * 4 + 0] = S[a].steps;
+      stats[a * 4 + 1] = S[a].restarts;
+      stats[a * 4 + 2] = S[a].bapplies;  // FP64 B applies of this instance
+      stats[a * 4 + 3] = S[a].cgits;     // inner CG iterations of this instance
+    }
+  if ((EV || res) && !(mixed && P.opt_refine)) {
     // one instance at a time through TMP (p columns available)
     for (int a = 0; a < na; ++a) {
       LzInst& I = S[a];

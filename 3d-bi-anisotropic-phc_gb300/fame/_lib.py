@@ -29,6 +29,10 @@ FAME_OPT_PRECOND = 0
 FAME_OPT_TOL32 = 1
 FAME_OPT_GRAPH = 2
 FAME_OPT_ITOL_FLOOR = 3
+FAME_OPT_PLANE_SPLIT = 4
+FAME_OPT_SIRA_NEAREST = 5
+FAME_OPT_REFINE = 6
+FAME_OPT_REFINE_TOL = 7
 FAME_SHAPE_WOODPILE, FAME_SHAPE_SPHERE, FAME_SHAPE_TETRA = 0, 1, 2
 FAME_RASTER_PAINT = 2
 
@@ -53,6 +57,7 @@ SIGNATURES = {
     "fame_set_option": (_i, [_vp, _i, _d]),
     "fame_sync": (_i, [_vp]),
     "fame_last_error": (C.c_char_p, [_vp]),
+    "fame_refine_residuals": (C.c_int, [_vp, C.POINTER(C.c_double), C.c_int]),
     "fame_plan_info": (_i, [_vp, _pi, _pi, _pll]),
     "fame_apply_A": (_i, [_vp, _i, _vp, _vp, _i, _pi, _i]),
     "fame_apply_B": (_i, [_vp, _i, _vp, _vp, _i, _pi, _i]),

@@ -55,6 +55,7 @@ def interior_modes(plan, nev, sigma, tol=1e-8, inner_tol=1e-3, no_restart=50, re
     """The `nev` eigenfrequencies of instance 0 closest to `sigma` (shifted SIRA,
     shift = sigma) with NFSEP and ORGSEP residuals and field maxima."""
     t0 = time.perf_counter()
+    plan.set_option("sira_nearest", 1)  # the pairs nearest sigma, on either side
     r = plan.jdsira(nev, target=sigma, shift=sigma, tol=tol, no_restart=no_restart, restart_dim=restart_dim,
                     inner_tol=inner_tol, inner_prec=inner_prec, want_vectors=True)
     torch.cuda.synchronize()

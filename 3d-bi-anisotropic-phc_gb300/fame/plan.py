@@ -207,9 +207,12 @@ class Plan:
         check(self._lib.fame_sync(self._h), self._h, "fame_sync")
 
     def set_option(self, option, value):
-        """fame_set_option: 'precond' (bool), 'tol32' (float), 'graph' (bool) or 'itol_floor' (float)."""
+        """fame_set_option: 'precond' (bool), 'tol32' (float), 'graph' (bool), 'itol_floor' (float),
+        'plane_split' (bool), 'sira_nearest' (bool), 'refine' (bool) or 'refine_tol' (float)."""
         code = {"precond": L.FAME_OPT_PRECOND, "tol32": L.FAME_OPT_TOL32, "graph": L.FAME_OPT_GRAPH,
-                "itol_floor": L.FAME_OPT_ITOL_FLOOR}.get(option, option)
+                "itol_floor": L.FAME_OPT_ITOL_FLOOR, "plane_split": L.FAME_OPT_PLANE_SPLIT,
+                "sira_nearest": L.FAME_OPT_SIRA_NEAREST, "refine": L.FAME_OPT_REFINE,
+                "refine_tol": L.FAME_OPT_REFINE_TOL}.get(option, option)
         check(self._lib.fame_set_option(self._h, int(code), float(value)), self._h, "fame_set_option")
         return self
 
@@ -358,7 +361,8 @@ class Plan:
                                     stats.ctypes.data_as(C.POINTER(C.c_longlong)))
         if rc not in (L.FAME_OK, L.FAME_ERR_NOT_CONVERGED):
             check(rc, self._h, "fame_lanczos")
-        return dict(ew=ew, omega=1.0 / ew, res=res, ev=ev, stats=stats, status=rc)
+        return dict(ew=ew, omega=1.0 / ew, res=res, ev=ev, stats=stats, status=rc,
+                    res_before=self.refine_residuals(res.shape))
 
     def jdsira(self, nev, target=0.0, tol=1e-8, no_restart=50, restart_dim=4, inner_tol=1e-2, inner_maxit=30000,
                inst=0, inner_prec="c64", want_vectors=False, shift=0.0):
@@ -404,4 +408,14 @@ class Plan:
                                        stats.ctypes.data_as(C.POINTER(C.c_longlong)))
         if rc not in (L.FAME_OK, L.FAME_ERR_NOT_CONVERGED):
             check(rc, self._h, "fame_band_solve")
-        return dict(ew=ew, omega=1.0 / ew, res=res, stats=stats, status=rc, ev=ev)
+        return dict(ew=ew, omega=1.0 / ew, res=res, stats=stats, status=rc, ev=ev,
+                    res_before=self.refine_residuals(res.shape))
+
+    def refine_residuals(self, shape=None):
+        """NFSEP residuals before the last FP64 refinement sweep (fame_refine_residuals), or None."""
+        n = self._lib.fame_refine_residuals(self._h, None, 0)
+        if n <= 0:
+            return None
+        out = np.zeros(n, dtype=np.float64)
+        self._lib.fame_refine_residuals(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), n)
+        return out.reshape(shape) if shape is not None and int(np.prod(shape)) == n else out

@@ -85,19 +85,43 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *   FAME_OPT_ITOL_FLOOR  mixed form: lower bound of the per-instance inner
  *                     tolerance, which is tightened by the spread of the
  *                     wanted Ritz values and starts there at near-zero wave
- *                     vectors [1e-13]. */
-enum fame_option { FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2, FAME_OPT_ITOL_FLOOR = 3 };
+ *                     vectors [1e-13].
+ *   FAME_OPT_PLANE_SPLIT  fncB plane kernels with several threads per FFT
+ *                     pencil on the grid sizes that have them [1]; 0 keeps
+ *                     one thread per pencil (same results to rounding).
+ *   FAME_OPT_SIRA_NEAREST  fame_jdsira's Ritz choice: 0 the reference's 'CL'
+ *                     (real Ritz values above the target, closest first;
+ *                     Choose_Ritz_Pair_Unsymm4.m:176-186) [0]; 1 the closest
+ *                     on either side of the target.
+ *   FAME_OPT_REFINE   mixed form (FAME_C64) of fame_lanczos / fame_band_solve:
+ *                     one FP64 refinement sweep of the converged Ritz pairs
+ *                     [1]: Y = B^-1 A X by the mixed inner solve, then FP64
+ *                     Rayleigh-Ritz on [X Y] per k-point; the returned
+ *                     eigenvalues, vectors and residuals are the refined ones
+ *                     (the residuals before: fame_refine_residuals).
+ *   FAME_OPT_REFINE_TOL  inner B^-1 tolerance of that sweep [1e-12]. */
+enum fame_option {
+  FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2, FAME_OPT_ITOL_FLOOR = 3, FAME_OPT_PLANE_SPLIT = 4,
+  FAME_OPT_SIRA_NEAREST = 5, FAME_OPT_REFINE = 6, FAME_OPT_REFINE_TOL = 7
+};
 int fame_set_option(fame_plan_t plan, int option, double value);
+
+/* NFSEP residuals ||B x - omega A x|| of the Ritz pairs before the FP64
+ * refinement sweep of the last mixed-form fame_lanczos / fame_band_solve on
+ * this plan ([nk][k] for a band solve); copies at most `n` of them to
+ * `before` and returns their count (0 when no sweep ran).  No reference
+ * counterpart. */
+int fame_refine_residuals(fame_plan_t plan, double* before, int n);
 
 /*
  * Autotuner (no reference counterpart): time the launch parameters of the
  * fncB sequence for precision `prec` and batch width `nvec` on this plan
  * (vectors per launch sequence: the whole batch, 1/2, 1/4, 1/8 of it or any
- * width up to 16;
- * threads per block of the stencil kernels: 128, 256, 512) and keep the
+ * width up to 16; the material stencil: 0 = single pass, or 128, 256, 512
+ * threads per block of the two-kernel form) and keep the
  * fastest for later calls with that width.  Outputs (may be NULL): the chosen
- * chunk (0 = whole batch), block size and the measured microseconds of one
- * fncB.  fame_set_tune installs a setting directly (e.g. from a cache).
+ * chunk (0 = whole batch), stencil setting and the measured microseconds of
+ * one fncB.  fame_set_tune installs a setting directly (e.g. from a cache).
  */
 int fame_autotune(fame_plan_t plan, int prec, int nvec, int* chunk, int* stencil_tpb, double* us);
 int fame_set_tune(fame_plan_t plan, int prec, int nvec, int chunk, int stencil_tpb);
@@ -119,7 +143,8 @@ int fame_apply_B(fame_plan_t plan, int prec, const void* x, void* y, int nvec, c
  * whose address is looked up on the first call on each device (make that call
  * before any stream capture).  x and y are device pointers, vector v belongs
  * to instance v % nk; requests needing more than 16 MiB of scratch
- * (nvec * 12 * n^3 * element size) are rejected with FAME_ERR_BAD_ARG.  All
+ * (nvec * 12 * n^3 * element size) are rejected with FAME_ERR_BAD_ARG.  The
+ * plan's device must be the current device (FAME_ERR_BAD_ARG otherwise).  All
  * calls share the array: calls whose kernels overlap on the GPU race.
  * No counterpart in the reference. */
 int fame_apply_B_noalloc(fame_plan_t plan, int prec, const void* x, void* y, int nvec);

@@ -32,6 +32,7 @@ __all__ = [
     "BandProblem", "build_problem", "woodpile_phases", "fft_workers",
     "field_diagonals", "build_problem_field", "material_quad_coeffs", "field_gradient",
     "chiral_noise_field", "lanczos_gep", "gsreorthog",
+    "gram_schmidt_ref", "choose_ritz_pair_cl", "sira_correction", "jdsira_driver4",
 ]
 
 _W = max(1, min(8, os.cpu_count() or 1))
@@ -955,3 +956,244 @@ def lanczos_gep(fA, fB, fBinv, n, k, m, itmax, tol, v0, bnorm_restart=False):
             ew, V = np.linalg.eigh(T)
             return Q[:, :k] @ V, ew, nit
     return None, None, nit
+
+
+# --------------------------------------------------------------------------
+# JD-SIRA with locking (light_locked_Huang/): Driver4, Locking4, the 'CL'
+# Ritz choice of Choose_Ritz_Pair_Unsymm4 and the SIRA correction
+# --------------------------------------------------------------------------
+def gram_schmidt_ref(Y):
+    """``light_locked_Huang/Gram_Schmidt.m:1-25``: modified Gram-Schmidt
+    dropping columns of norm <= 1e-6.  Returns the orthonormal columns."""
+    Y = np.array(Y, dtype=np.complex128, copy=True)
+    nq = 0
+    for k in range(Y.shape[1]):
+        t = np.linalg.norm(Y[:, k])
+        if abs(t) > 1.0e-6:
+            Y[:, nq] = Y[:, k] / t
+            for j in range(k + 1, Y.shape[1]):
+                Y[:, j] = Y[:, j] - np.vdot(Y[:, nq], Y[:, j]) * Y[:, nq]
+            nq += 1
+    return Y[:, :nq]
+
+
+def _close_within(a, b, tol, kmax):
+    """``|a - b| <= 10^k tol`` for some k in -1..kmax (the ladder of
+    Choose_Ritz_Pair_Unsymm4.m:30-37,62-69,92-99)."""
+    return any(abs(a - b) <= 10.0 ** k * tol for k in range(-1, kmax + 1))
+
+
+def choose_ritz_pair_cl(iteno, ew, ew_order, target, VRR, tol, rppd, locked):
+    """``light_locked_Huang/Choose_Ritz_Pair_Unsymm4.m:1-302`` for
+    ``Choose_Type = 'CL'`` (the drivers' choice) with ``target_org == target``:
+    Ritz values that repeat locked eigenvalues are removed with their
+    multiplicities (:24-166), candidates are the real Ritz values above the
+    target (:176-186), the closest ``ewno <= rppd`` are taken in order
+    (:236-272) and the rest of the restart block is filled by distance
+    (:274-301).  Returns ``(ewno, ritz_ew, ritz_ev)`` (columns normalised)."""
+    sort_ritz = np.array(ew, dtype=np.complex128, copy=True)
+    if ew_order > 1 and len(locked):
+        sort_ew = np.array(locked, dtype=np.complex128, copy=True)
+        nl = len(sort_ew)
+        mult_cn = np.zeros(nl, dtype=int)
+        for i in range(nl):                                              # :25-50
+            if sort_ew[i].real > -1.0e13:
+                c = 1
+                for i1 in range(i + 1, nl):
+                    if sort_ew[i1].real > -1.0e13 and _close_within(sort_ew[i1], sort_ew[i], tol, 1):
+                        c += 1
+                        sort_ew[i1] = -1.0e14
+                mult_cn[i] = c
+        idx_w = np.zeros(iteno, dtype=int)                               # 1-based owner, 0 = first
+        mult_w = np.zeros(iteno, dtype=int)
+        for i in range(iteno):                                           # :56-82
+            if idx_w[i] == 0:
+                c = 1
+                for i1 in range(i + 1, iteno):
+                    if idx_w[i1] == 0 and _close_within(sort_ritz[i1], sort_ritz[i], tol, 1):
+                        c += 1
+                        idx_w[i1] = i + 1
+                mult_w[i] = c
+        for i in range(nl):                                              # :84-166
+            if sort_ew[i].real <= -1.0e13:
+                continue
+            ind = None
+            for i1 in range(iteno):
+                if idx_w[i1] == 0 and _close_within(sort_ritz[i1], sort_ew[i], tol, 5):
+                    ind = i1
+                    break
+            if ind is None:
+                continue
+            owned = [jj for jj in range(iteno) if idx_w[jj] == ind + 1]
+            if mult_cn[i] >= mult_w[ind]:
+                sort_ritz[ind] = 1.0e14
+                for jj in owned:
+                    sort_ritz[jj] = 1.0e14
+            else:
+                grp = [ind] + owned
+                ld = [np.linalg.norm(VRR[ew_order - 1:iteno, g]) for g in grp]
+                for _ in range(mult_cn[i]):
+                    kk = int(np.argmin(ld))
+                    sort_ritz[grp[kk]] = 1.0e14
+                    ld[kk] = 1.0e14
+            idx_w[ind] = -1
+    cand, dist = [], []
+    for i in range(iteno):                                               # :176-186 ('CL')
+        if abs(sort_ritz[i]) < 1.0e10:
+            e = ew[i]
+            if (abs(e.real) < 1e-4 and e.imag > 1e-3) or (e.real > np.real(target) and abs(e.imag) < 1e-8):
+                cand.append(i)
+                dist.append(abs(e.real - np.real(target)))
+    if not cand:                                                         # :218-224
+        cand = list(range(iteno))
+        dist = [abs(sort_ritz[i] - target) for i in range(iteno)]
+    dist = np.array(dist, dtype=float)
+    ewno = min(len(cand), rppd)
+    picked, ritz_ew, ritz_ev = [], [], []
+    for _ in range(ewno):                                                # :236-272
+        k = int(np.argmin(dist))
+        picked.append(cand[k])
+        ritz_ew.append(ew[cand[k]])
+        v = VRR[:iteno, cand[k]]
+        ritz_ev.append(v / np.linalg.norm(v))
+        dist[k] = 1.0e14
+    if ewno < rppd:                                                      # :274-301
+        rest = [i for i in range(iteno) if i not in picked and abs(sort_ritz[i]) < 1.0e10]
+        rest.sort(key=lambda i: abs(ew[i] - target))
+        for i in rest[:rppd - ewno]:
+            ritz_ew.append(ew[i])
+            v = VRR[:iteno, i]
+            ritz_ev.append(v / np.linalg.norm(v))
+        ewno += min(rppd - ewno, len(rest))
+    return ewno, np.array(ritz_ew), np.stack(ritz_ev, axis=1)
+
+
+def sira_correction(A, rhs, tol, maxit, B=None, shift=0.0):
+    """``SIRA_solve_residual_LS_GEP.m:54`` with ``LS_solver = 'minres'``:
+    MINRES on ``GEP_shift_mtx_prod_vec`` (``Jacobi_Davidson/GEP_shift_mtx_prod_vec.m:28-29``),
+    which applies ``A`` alone (its ``- sigma*B`` term is commented out;
+    ``shift`` restores it).  ``minres1`` is not in the reference tree, so
+    SciPy's MINRES (relative tolerance ``tol``) stands in for it.
+    Returns ``(t, iters)``."""
+    import scipy.sparse.linalg as spla
+    n = rhs.shape[0]
+
+    def mv(v):
+        v = np.asarray(v).ravel()
+        y = A(v)
+        return y - shift * B(v) if shift != 0.0 else y
+
+    op = spla.LinearOperator((n, n), matvec=mv, dtype=np.complex128)
+    its = [0]
+
+    def cb(_):
+        its[0] += 1
+
+    t, _ = spla.minres(op, rhs, rtol=tol, maxiter=maxit, callback=cb)
+    return t, its[0]
+
+
+def jdsira_driver4(A, B, mtxdim, no_restart, ew_number, tol, initial_vec, target, ls_tol=1e-2, ls_maxit=30000,
+                   shift=0.0, max_outer=6000):
+    """``GEP_AB_Herm_JDSIRA_Driver4.m:12-80`` with
+    ``GEP_AB_Herm_JDSIRA_Locking4.m:91-505`` (target type 'CL', correction
+    'SIRA' by MINRES without preconditioner, as
+    ``main_EIG_np_sphere_n60_gamma3p46427.m:111-125`` calls it with
+    ``A = fncB``, ``B = fncA``): the ``ew_number`` eigenpairs of
+    ``A x = theta B x`` selected by the 'CL' rule around ``target``.
+
+    Per outer step: projected pencil ``eig(V'AV, V'BV)`` (:96-121), Ritz
+    choice, unit Ritz vector and residual ``r = A u - theta B u`` (:181-185),
+    acceptance at ``rsdl <= tol`` or after five steps in ``(tol, 10 tol]``
+    (:198-208), else ``t = minres(A, r)`` orthogonalised against V by
+    classical Gram-Schmidt and appended (:262-312); restart keeps the locked
+    vectors, the current Ritz vector and three more (:327-345); after
+    convergence the pair is locked with every other Ritz pair already below
+    ``tol`` (:346-505).  Returns ``(EW, EV, stats)`` with ``stats`` the
+    outer steps and MINRES iterations."""
+    import scipy.linalg as sla
+    rppd = max(4, initial_vec.shape[1] if initial_vec.ndim == 2 else 1)
+    iv = initial_vec.reshape(mtxdim, -1).astype(np.complex128)
+    init = np.zeros((mtxdim, ew_number + rppd - 1), dtype=np.complex128)
+    init[:, :iv.shape[1]] = iv
+    proj = iv.shape[1]
+    locked_ew, EV = [], []
+    outer_total, inner_total = 0, 0
+    ew_order = 1
+    while ew_order <= ew_number:
+        # --- Locking4
+        V = np.zeros((mtxdim, no_restart + 2), dtype=np.complex128)
+        V[:, :proj] = init[:, :proj]
+        stop = False
+        no_near = 0
+        dim_eigsp = len(locked_ew)
+        ep = 1
+        while ep <= max_outer and not stop:
+            AV = np.stack([A(V[:, i]) for i in range(proj)], axis=1)
+            BV = np.stack([B(V[:, i]) for i in range(proj)], axis=1)
+            iteno = proj
+            while iteno <= no_restart and not stop:
+                # lower triangles of V'AV, V'BV, mirrored (:96-110)
+                M = V[:, :iteno].conj().T @ AV[:, :iteno]
+                Lm = V[:, :iteno].conj().T @ BV[:, :iteno]
+                M = np.tril(M) + np.tril(M, -1).conj().T
+                Lm = np.tril(Lm) + np.tril(Lm, -1).conj().T
+                ew, VRR = sla.eig(M, Lm)
+                ewno, ritz_ew, ritz_ev = choose_ritz_pair_cl(iteno, ew, ew_order, target, VRR, tol, rppd,
+                                                             locked_ew)
+                u = V[:, :iteno] @ ritz_ev[:, 0]
+                u = u / np.linalg.norm(u)
+                rv = A(u) - ritz_ew[0] * B(u)
+                rsdl = np.linalg.norm(rv)
+                no_near = no_near + 1 if (tol < rsdl <= 10.0 * tol) else 0
+                if rsdl <= tol or no_near >= 5:
+                    stop = True
+                elif iteno + 1 <= dim_eigsp + no_restart:
+                    t, its = sira_correction(A, rv, ls_tol, ls_maxit, B, shift)
+                    inner_total += its
+                    for j in range(iteno):
+                        t = t - np.vdot(V[:, j], t) * V[:, j]
+                    V[:, iteno] = t / np.linalg.norm(t)
+                    AV = np.concatenate([AV, A(V[:, iteno])[:, None]], axis=1)
+                    BV = np.concatenate([BV, B(V[:, iteno])[:, None]], axis=1)
+                iteno += 1
+                ep += 1
+                outer_total += 1
+            if not stop:                                                 # :327-345 restart
+                iteno -= 1
+                jj = min(rppd - 1, ew_number + rppd - 1)
+                keep = V[:, :iteno] @ ritz_ev[:iteno, 1:jj + 1]
+                W = np.concatenate([V[:, :dim_eigsp], u[:, None], keep], axis=1)
+                Q = gram_schmidt_ref(W)
+                proj = Q.shape[1]
+                V[:, :] = 0
+                V[:, :proj] = Q
+                init[:, :proj] = Q
+        # --- lock the converged pair and every other Ritz pair below tol (:346-505)
+        others, conv = [], []
+        for i in range(1, ewno):
+            w = V[:, :iteno - 1] @ ritz_ev[:iteno - 1, i]
+            w = w / np.linalg.norm(w)
+            r_i = np.linalg.norm(A(w) - ritz_ew[i] * B(w))
+            others.append(w)
+            conv.append(r_i <= tol)
+        Vl = [V[:, i] for i in range(dim_eigsp)]
+        Vl.append(u / np.linalg.norm(u))
+        EV.append(u / np.linalg.norm(u))
+        locked_ew.append(ritz_ew[0])
+        j = 0
+        for w, c, ri in zip(others, conv, ritz_ew[1:]):
+            if c:
+                Vl.append(w)
+                EV.append(w)
+                locked_ew.append(ri)
+                j += 1
+        for w, c in zip(others, conv):
+            if not c:
+                Vl.append(w)
+        Q = gram_schmidt_ref(np.stack(Vl, axis=1))
+        proj = min(Q.shape[1], ew_number + rppd - 1)
+        init[:, :proj] = Q[:, :proj]
+        ew_order += j + 1
+    EW = np.array(locked_ew[:ew_number])
+    return EW, np.stack(EV[:ew_number], axis=1), {"outer": outer_total, "minres": inner_total}

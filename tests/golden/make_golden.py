@@ -9,6 +9,14 @@ generator whose stream could change between NumPy versions).
 
     python tests/golden/make_golden.py          # rewrites woodpile_golden.npz
     python tests/golden/make_golden.py --n24    # rewrites woodpile_n24_X.npz (~3 min)
+    python tests/golden/make_golden.py --n60ops # operator digests at n = 60 (~1 min)
+    python tests/golden/make_golden.py --n60eig # FP64 Lanczos at n = 60, X (~40 min)
+
+At n = 60 one complex128 vector is 13.8 MB, so the n = 60 fixtures keep a
+digest of each output instead of the vector: its values at 1024 fixed
+indices, its inner products with four closed-form sketch vectors, and its
+norm (`digest`).  A wrong entry anywhere changes the sketches; the sampled
+values localise it.
 """
 from __future__ import annotations
 
@@ -26,6 +34,11 @@ import oracle as O  # noqa: E402
 
 FILE = os.path.join(HERE, "woodpile_golden.npz")
 N24_FILE = os.path.join(HERE, "woodpile_n24_X.npz")  # the first workload: n = 24, X point, 10 bands
+N60_OPS_FILE = os.path.join(HERE, "woodpile_n60_ops.npz")  # operator digests at the benchmark size
+N60_EIG_FILE = os.path.join(HERE, "woodpile_n60_X.npz")    # FP64 eigenvalues at the benchmark size
+N60_LABELS = ("X", "L")
+N60_SAMPLES = 1024
+N60_SKETCHES = 4
 CASES = [(4, "X"), (6, "X"), (6, "L")]   # operator fixtures
 EIG_CASES = [(6, "X"), (6, "L")]          # Lanczos fixtures: k = 4, p = 8, tol 1e-10
 BANDS = 4
@@ -36,6 +49,78 @@ def det_vec(length: int, s: int) -> np.ndarray:
     """A deterministic complex test vector."""
     j = np.arange(length, dtype=np.float64)
     return np.cos(0.731 * j + 0.37 * s) + 1j * np.sin(1.217 * j + 0.11 * s)
+
+
+def sample_index(length: int) -> np.ndarray:
+    """The fixed indices a digest samples (a stride coprime to every vector length used)."""
+    return np.unique((np.arange(N60_SAMPLES, dtype=np.int64) * 104729 + 17) % length)
+
+
+def digest(y: np.ndarray) -> dict:
+    """Sampled values, sketch inner products <s_j, y> and the norm of y."""
+    y = np.asarray(y, dtype=np.complex128).ravel()
+    L = y.shape[0]
+    sk = np.array([np.vdot(det_vec(L, 1000 + j), y) for j in range(N60_SKETCHES)])
+    return {"samp": y[sample_index(L)], "sketch": sk, "norm": np.array([np.linalg.norm(y)])}
+
+
+def digest_relerr(y: np.ndarray, ref: dict) -> float:
+    """Largest relative deviation of y's digest from a stored one (each part
+    relative to the reference's own scale: ||samples||, ||s_j||*||y||, ||y||)."""
+    d = digest(y)
+    L = np.asarray(y).size
+    e1 = np.linalg.norm(d["samp"] - ref["samp"]) / np.linalg.norm(ref["samp"])
+    e2 = np.max(np.abs(d["sketch"] - ref["sketch"])) / (np.sqrt(L) * ref["norm"][0])
+    e3 = abs(d["norm"][0] - ref["norm"][0]) / ref["norm"][0]
+    return float(max(e1, e2, e3))
+
+
+def n60_ops_inputs(n: int = 60):
+    Nq = n ** 3
+    return det_vec(4 * Nq, n), det_vec(3 * Nq, n + 1)
+
+
+N60_OPS = ("Bx", "Ax", "Tn", "Tt", "Pr", "Qr", "Prs", "Qrs")
+
+
+def compute_n60_ops(n: int = 60):
+    """fncB, fncA, MtxVecMul_FFT both ways and the Pr/Qr/Prs/Qrs handles of the
+    woodpile at n = 60 (X and L), as digests."""
+    out = {}
+    x, y3 = n60_ops_inputs(n)
+    Nq = n ** 3
+    for lab in N60_LABELS:
+        P = O.build_problem(n, wave_vec=O.fcc_vertex(lab))
+        outs = {
+            "Bx": P.B(x), "Ax": P.A(x),
+            "Tn": O.mtxvecmul_fft(y3, P.dims, "notranspose", P.svd.S, P.svd.D),
+            "Tt": O.mtxvecmul_fft(y3, P.dims, "transpose", P.svd.S, P.svd.D),
+            "Pr": P.fnc.Pr(x[:2 * Nq]), "Qr": P.fnc.Qr(x[2 * Nq:]),
+            "Prs": P.fnc.Prs(y3), "Qrs": P.fnc.Qrs(y3),
+        }
+        out[f"{lab}_theta"] = np.asarray(P.thetas, dtype=np.float64)
+        for name, y in outs.items():
+            for part, v in digest(y).items():
+                out[f"{lab}_{name}_{part}"] = v
+    return out
+
+
+def n60_ref(fix, lab: str, name: str) -> dict:
+    return {part: fix[f"{lab}_{name}_{part}"] for part in ("samp", "sketch", "norm")}
+
+
+def compute_n60_eig(k=10):
+    """The woodpile at n = 60 and the X point: the 10 largest eigenvalues of
+    B^-1 A by the oracle's Lanczos.m (p = 2k, tol 1e-10, inner pcg 1e-12),
+    as band_structure_woodpile_Lanczos_n60_gamma0p2.m:74-81 runs each k-point."""
+    O.fft_workers(os.cpu_count() or 1)
+    P = O.build_problem(60, wave_vec=O.fcc_vertex("X"))
+    L = 4 * 60 ** 3
+    nits = []
+    _, ew, it = O.lanczos(P.A, P.B, lambda r: O.fncinvB(r, P.B, 1e-12, 10000, stats=nits), L, k, 1e-10, 10000,
+                          2 * k, np.ones(L, complex))
+    return {"ew": np.asarray(ew, dtype=np.float64), "theta": np.asarray(P.thetas, dtype=np.float64),
+            "lanczos_steps": np.array([it]), "pcg_iters": np.array([int(np.sum(nits))])}
 
 
 def images(A):
@@ -96,7 +181,13 @@ def compute_n24(k=10):
 
 
 if __name__ == "__main__":
-    if "--n24" in sys.argv:
+    if "--n60ops" in sys.argv:
+        np.savez_compressed(N60_OPS_FILE, **compute_n60_ops())
+        print("wrote", N60_OPS_FILE, os.path.getsize(N60_OPS_FILE), "bytes")
+    elif "--n60eig" in sys.argv:
+        np.savez_compressed(N60_EIG_FILE, **compute_n60_eig())
+        print("wrote", N60_EIG_FILE, os.path.getsize(N60_EIG_FILE), "bytes")
+    elif "--n24" in sys.argv:
         np.savez_compressed(N24_FILE, **compute_n24())
         print("wrote", N24_FILE, os.path.getsize(N24_FILE), "bytes")
     else:

@@ -30,7 +30,9 @@ def test_jdsira_matches_dense_spectrum(cuda, fame_lib, target, gamma, inner_prec
     n, nev = 4, 5
     kvec = fame.fcc_point("X")
     th = dense_thetas(n, kvec, gamma)
-    ref = th[np.argsort(np.abs(th - target))][:nev]
+    # 'CL' (Choose_Ritz_Pair_Unsymm4.m:176-186): the eigenvalues above the target, closest first
+    above = np.sort(th[th > target])
+    ref = above[:nev]
     plan = fame.woodpile_plan(n, [kvec], gamma=gamma)
     # the reference's correction drops the shift (fine for target 0); an interior
     # target uses the shifted correction

@@ -3,12 +3,17 @@ device memory at call time (a MEX gateway under MATLAB's gpuArray memory
 manager, an application pooling its whole device budget).  It draws its
 scratch from one fixed 16 MiB device array instead of the plan's on-demand
 scratch.  Checked through the C ABI against fame_apply_B on two calls in a
-row (the array keeps the previous call's contents between them)."""
+row (the array keeps the previous call's contents between them), against
+the oracle's fncB (fun_Lanczos/fncB.m:3-6), and on a plan whose fncB runs in
+sub-batches (the layout that places the second work buffer inside the fixed
+array)."""
 import ctypes as C
 
+import numpy as np
 import pytest
 
 import fame
+import oracle as O
 from problems import Pair, relerr
 
 pytestmark = pytest.mark.gpu
@@ -41,6 +46,38 @@ def test_noalloc_matches_apply_B_twice(cuda, fame_lib, prec):
         got = _noalloc(P.plan, x).cpu().numpy()
         torch.cuda.synchronize()
         assert relerr(got, ref) < TOL[prec], (call, relerr(got, ref))
+        xh = x.cpu().numpy().astype(np.complex128)
+        for v in range(xh.shape[0]):
+            svd, fnc, mat = P.ref(v % P.nk)
+            assert relerr(got[v], O.fncB(xh[v], fnc, mat)) < TOL[prec], (call, v)
+
+
+@pytest.mark.parametrize("prec", ["c64", "c128"])
+def test_noalloc_sub_batches(cuda, fame_lib, prec):
+    """fncB in sub-batches of 2 vectors (as the autotuner may choose), so each
+    sub-batch reuses the front of both work buffers of the fixed array."""
+    import torch
+
+    dt = torch.complex128 if prec == "c128" else torch.complex64
+    P = Pair(12, nk=3, seed=5)
+    P.plan.set_tune(prec, 6, 2, 0)
+    for call in range(2):
+        x = torch.from_numpy(P.vec(4 * P.Nq, 6)).to(device="cuda", dtype=dt)
+        ref = P.plan.apply_B(x).cpu().numpy()
+        got = _noalloc(P.plan, x).cpu().numpy()
+        assert relerr(got, ref) < TOL[prec], (call, relerr(got, ref))
+    P.plan.set_tune(prec, 6, 0, 256)
+    x = torch.from_numpy(P.vec(4 * P.Nq, 6)).to(device="cuda", dtype=dt)
+    t = P.plan.autotune(6, prec=prec)
+    got = _noalloc(P.plan, x).cpu().numpy()
+    assert relerr(got, P.plan.apply_B(x).cpu().numpy()) < TOL[prec], t
+
+
+def test_noalloc_null_plan_sets_error(cuda, fame_lib):
+    lib = fame.load()
+    rc = lib.fame_apply_B_noalloc(None, 1, None, None, 1)
+    assert rc == 1
+    assert b"null plan" in lib.fame_last_error(None)
 
 
 def test_noalloc_rejects_oversized(cuda, fame_lib):
