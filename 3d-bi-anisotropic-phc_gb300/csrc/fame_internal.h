@@ -85,7 +85,7 @@ struct Plan {
   int opt_plane_split = 1;            // fncB plane kernels with several threads per pencil where compiled
   int opt_sira_nearest = 0;           // SIRA Ritz choice: 0 'CL' (above the target), 1 nearest either side
   int opt_refine = 1;                 // mixed form: FP64 refinement sweep of the Ritz pairs
-  double opt_refine_tol = 1e-12;      // its inner B^{-1} tolerance
+  double opt_refine_tol = 1e-6;       // relative tolerance of its correction solve B^{-1} R
   std::vector<double> refine_res_before;  // NFSEP residuals before the last refinement sweep
   std::vector<double> theta;          // [nk][3]
   std::vector<double> sigma_min;      // [nk] smallest curl singular value sqrt(min |L|^2)

@@ -342,19 +342,26 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
 
 // ---------------------------------------------------------------------------
 // FP64 refinement sweep of converged Ritz pairs (no reference counterpart:
-// the reference's FP64 Lanczos needs none).  For the k Ritz vectors X of
-// every instance, batched over all instances:
-//   Y = B^{-1} A X               mixed-precision inner solve to `tol`
-//   [X Y]^H A [X Y] c = lambda [X Y]^H B [X Y] c     FP64 Rayleigh-Ritz
-// (one step of block inverse iteration with Rayleigh-Ritz on the doubled
-// space), keeping the k largest lambda, as Lanczos.m:109 orders them.  The
-// NFSEP residual ||B x - omega A x|| (EvaluteError_Chiral_no_inv.m:20, x
-// B-normalised, omega = 1/lambda) is evaluated in FP64 before and after.
+// the reference's FP64 Lanczos needs none).  For the k Ritz pairs (Lambda, X)
+// of every instance, batched over all instances:
+//   R = A X - B X Lambda                      FP64 residuals
+//   W = B^{-1} R                              mixed-precision inner solve to `tol`
+//   [X W]^H A [X W] c = lambda [X W]^H B [X W] c    FP64 Rayleigh-Ritz
+// W spans the same space as B^{-1} A X beside X (one step of block inverse
+// iteration) without its cancellation: for converged pairs B^{-1} A X is
+// X Lambda to many digits.  The pencil is reduced to the B-orthonormal basis
+// of the well-conditioned part of [X W] (canonical orthogonalisation: the
+// eigenvectors of [X W]^H B [X W] with eigenvalues above 1e-13 of the
+// largest), and the k largest lambda are kept, as Lanczos.m:109 orders them.
+// The NFSEP residual ||B x - omega A x|| (EvaluteError_Chiral_no_inv.m:20,
+// x B-normalised, omega = 1/lambda) is evaluated in FP64 before and after;
+// a pair keeps its old value when the sweep would not lower its residual.
 // X: [na*k][4Nq] B-normalised Ritz vectors, overwritten by the refined ones;
 // lam: [na][k] in and out.
 // ---------------------------------------------------------------------------
 int ritz_refine(Plan& P, const std::vector<int>& insts, int k, double2* X, double* lam, double* res_before,
                 double* res_after, double tol, long long* b64_vec, long long* cg_vec) {
+  using cd = std::complex<double>;
   const int na = (int)insts.size();
   if (na == 0 || k < 1) return FAME_OK;
   cudaStream_t st = P.stream;
@@ -366,17 +373,19 @@ int ritz_refine(Plan& P, const std::vector<int>& insts, int k, double2* X, doubl
   FAME_CK(e, "refine workspace");
   double2* BX = (double2*)workspace(P, WS_RF_BX, cb * nv, &e);
   FAME_CK(e, "refine workspace");
-  double2* Y = (double2*)workspace(P, WS_RF_Y, cb * nv, &e);
+  double2* W = (double2*)workspace(P, WS_RF_Y, cb * nv, &e);
   FAME_CK(e, "refine workspace");
-  double2* BY = (double2*)workspace(P, WS_RF_BY, cb * nv, &e);
+  double2* BW = (double2*)workspace(P, WS_RF_BY, cb * nv, &e);
   FAME_CK(e, "refine workspace");
-  double2* AY = (double2*)workspace(P, WS_RF_AY, cb * nv, &e);
+  double2* AW = (double2*)workspace(P, WS_RF_AY, cb * nv, &e);
+  FAME_CK(e, "refine workspace");
+  double2* Rv = (double2*)workspace(P, WS_RF_R, cb * nv, &e);
   FAME_CK(e, "refine workspace");
   double2* Z = (double2*)workspace(P, WS_RF_Z, cb * 2 * k, &e);
   FAME_CK(e, "refine workspace");
   int* dinst = (int*)workspace(P, WS_RF_INST, sizeof(int) * nv + 64, &e);
   FAME_CK(e, "refine workspace");
-  const int ncall = 8 * k;  // (A, B) x (X rows, Y rows) x 2k columns
+  const int ncall = 8 * k;  // (A, B) x (X rows, W rows) x 2k columns
   double2* G = (double2*)workspace(P, WS_RF_G, sizeof(double2) * ((size_t)ncall * na * k + 4 * nv) + 64, &e);
   FAME_CK(e, "refine workspace");
   double2* scal = G + (size_t)ncall * na * k;  // [2][nv] axpby scalars, [nv] norms
@@ -395,45 +404,70 @@ int ritz_refine(Plan& P, const std::vector<int>& insts, int k, double2* X, doubl
   ctx.nk = P.nk;
   double2* W0 = (double2*)P.d_work;
   double2* W1 = W0 + (size_t)nv * 6 * P.Nq;
-  // NFSEP residuals of (lam, V) with AV, BV given: R = BV - (1/lam) AV (into AY)
-  auto nfsep = [&](const double2* AV, const double2* BV, const double* lm, double* out) -> int {
+  // out = s1 * V1 + s2 * V2 per vector (s1, s2 real, per vector)
+  auto combine = [&](const double2* V1, const std::vector<double>& s1, const double2* V2,
+                     const std::vector<double>& s2, double2* out) -> int {
     std::vector<double2> ab(2 * (size_t)nv);
     for (int i = 0; i < nv; ++i) {
-      ab[i] = make_double2(1.0, 0.0);
-      ab[nv + i] = make_double2(-1.0 / lm[i], 0.0);
+      ab[i] = make_double2(s1[i], 0.0);
+      ab[nv + i] = make_double2(s2[i], 0.0);
     }
-    FAME_CK(h2d_async(P, scal, ab.data(), sizeof(double2) * 2 * nv), "refine residual");
-    FAME_CK(cudaMemcpyAsync(AY, AV, cb * nv, cudaMemcpyDeviceToDevice, st), "refine residual");
-    FAME_CK(axpby_batched<double>(BV, AY, L, L, nv, scal, scal + nv, nullptr, st), "refine residual");
-    FAME_CK(dot_batched<double>(AY, L, 0, 1, AY, L, L, nv, scal + 2 * nv, part, nblk, nullptr, st), "refine residual");
+    FAME_CK(h2d_async(P, scal, ab.data(), sizeof(double2) * 2 * nv), "refine combine");
+    if (out != V2) FAME_CK(cudaMemcpyAsync(out, V2, cb * nv, cudaMemcpyDeviceToDevice, st), "refine combine");
+    FAME_CK(axpby_batched<double>(V1, out, L, L, nv, scal, scal + nv, nullptr, st), "refine combine");
+    return FAME_OK;
+  };
+  auto norms = [&](const double2* V, double* out) -> int {
+    FAME_CK(dot_batched<double>(V, L, 0, 1, V, L, L, nv, scal + 2 * nv, part, nblk, nullptr, st), "refine norm");
     std::vector<double2> h(nv);
-    FAME_CK(cudaMemcpyAsync(h.data(), scal + 2 * nv, sizeof(double2) * nv, cudaMemcpyDeviceToHost, st), "refine residual");
-    FAME_CK(cudaStreamSynchronize(st), "refine residual");
+    FAME_CK(cudaMemcpyAsync(h.data(), scal + 2 * nv, sizeof(double2) * nv, cudaMemcpyDeviceToHost, st), "refine norm");
+    FAME_CK(cudaStreamSynchronize(st), "refine norm");
     for (int i = 0; i < nv; ++i) out[i] = std::sqrt(std::max(0.0, h[i].x));
     return FAME_OK;
   };
-  // A X, B X and the residuals before
+  std::vector<double> ones(nv, 1.0), mlam(nv), mom(nv);
+  // A X, B X; NFSEP before: || B X - omega A X ||, the GEP residual A X - B X Lambda
   FAME_CK(launch_fncA<double>(P, X, AX, nv, ctx, st), "refine fncA");
   FAME_CK(launch_fncB<double>(P, X, BX, nv, ctx, W0, W1, st), "refine fncB");
-  for (int i = 0; i < nv; ++i) b64_vec[i]++;
+  for (int i = 0; i < nv; ++i) {
+    b64_vec[i]++;
+    mlam[i] = -lam[i];
+    mom[i] = -1.0 / lam[i];
+  }
+  int rc;
   std::vector<double> rb(nv);
-  int rc = nfsep(AX, BX, lam, rb.data());
-  if (rc) return rc;
+  if ((rc = combine(AX, mom, BX, ones, Rv))) return rc;  // Rv = BX - omega AX
+  if ((rc = norms(Rv, rb.data()))) return rc;
   if (res_before) std::copy(rb.begin(), rb.end(), res_before);
-  // Y = B^{-1} A X (FP64-accurate mixed solve), A Y
+  if ((rc = combine(BX, mlam, AX, ones, Rv))) return rc;  // Rv = AX - lambda BX
+  // W = B^{-1} R (a search direction: its accuracy does not limit the sweep,
+  // whose Rayleigh-Ritz uses exact FP64 applies of A and B on W)
   long long cgi = 0, b64 = 0;
-  rc = solve_B_mixed(P, AX, Y, BY, nv, dinst, tol, 8, P.opt_tol32, 4000, nullptr, &cgi, &b64, nullptr, cg_vec,
+  rc = solve_B_mixed(P, Rv, W, BW, nv, dinst, tol, 8, P.opt_tol32, 4000, nullptr, &cgi, &b64, nullptr, cg_vec,
                      b64_vec);
   if (rc == FAME_ERR_NAN || rc == FAME_ERR_BREAKDOWN) return rc;
-  FAME_CK(launch_fncA<double>(P, Y, AY, nv, ctx, st), "refine fncA");
-  // Gram matrices G_A = Z^H A Z, G_B = Z^H B Z per instance, Z = [X_a Y_a]:
-  // call c = ((op * 2 + rowblk) * 2k + col) fills G[c][a][0..k)
-  const long long vs = (long long)k * L;  // instance stride inside X, Y, AX, ...
+  // W to unit B-norm (its norm is that of the residuals, ~1e-10, and would
+  // otherwise vanish below the cut-off of the orthogonalisation)
+  {
+    FAME_CK(dot_batched<double>(W, L, 0, 1, BW, L, L, nv, scal + 2 * nv, part, nblk, nullptr, st), "refine wnorm");
+    std::vector<double2> h(nv);
+    FAME_CK(cudaMemcpyAsync(h.data(), scal + 2 * nv, sizeof(double2) * nv, cudaMemcpyDeviceToHost, st), "refine wnorm");
+    FAME_CK(cudaStreamSynchronize(st), "refine wnorm");
+    std::vector<double> sw(nv);
+    for (int i = 0; i < nv; ++i) sw[i] = h[i].x > 0.0 && std::isfinite(h[i].x) ? 1.0 / std::sqrt(h[i].x) : 0.0;
+    double* dsw = (double*)(scal + 3 * nv);
+    FAME_CK(h2d_async(P, dsw, sw.data(), sizeof(double) * nv), "refine wnorm");
+    FAME_CK(scale_batched<double>(W, W, L, nv, dsw, nullptr, st), "refine wnorm");
+    FAME_CK(scale_batched<double>(BW, BW, L, nv, dsw, nullptr, st), "refine wnorm");
+  }
+  FAME_CK(launch_fncA<double>(P, W, AW, nv, ctx, st), "refine fncA");
+  // Gram matrices on Z = [X_a W_a]: call c = ((op * 2 + rowblk) * 2k + col) fills G[c][a][0..k)
+  const long long vs = (long long)k * L;  // instance stride inside X, W, AX, ...
   for (int op = 0; op < 2; ++op)
     for (int rb2 = 0; rb2 < 2; ++rb2)
       for (int col = 0; col < 2 * k; ++col) {
-        const double2* rows = rb2 == 0 ? X : Y;
-        const double2* cv = op == 0 ? (col < k ? AX : AY) : (col < k ? BX : BY);
+        const double2* rows = rb2 == 0 ? X : W;
+        const double2* cv = op == 0 ? (col < k ? AX : AW) : (col < k ? BX : BW);
         cv += (size_t)(col % k) * L;
         const int c = (op * 2 + rb2) * 2 * k + col;
         FAME_CK(dot_batched<double>(rows, vs, L, k, cv, vs, L, na, G + (size_t)c * na * k, part, nblk, nullptr, st),
@@ -443,62 +477,112 @@ int ritz_refine(Plan& P, const std::vector<int>& insts, int k, double2* X, doubl
   FAME_CK(cudaMemcpyAsync(hG.data(), G, sizeof(double2) * hG.size(), cudaMemcpyDeviceToHost, st), "refine gram");
   FAME_CK(cudaStreamSynchronize(st), "refine gram");
   const int m = 2 * k;
-  std::vector<double2> hC((size_t)na * m * k);
-  std::vector<double> lam_new((size_t)nv);
+  std::vector<double2> hC((size_t)na * m * k, make_double2(0.0, 0.0));
+  std::vector<double> lam_new(lam, lam + nv);
   for (int a = 0; a < na; ++a) {
-    std::vector<std::complex<double>> GA((size_t)m * m), GB((size_t)m * m);
+    std::vector<cd> GA((size_t)m * m), GB((size_t)m * m);
     for (int op = 0; op < 2; ++op)
       for (int rb2 = 0; rb2 < 2; ++rb2)
         for (int col = 0; col < m; ++col) {
           const int c = (op * 2 + rb2) * m + col;
           for (int r = 0; r < k; ++r) {
-            const double2 v = hG[((size_t)c * na + a) * k + r];  // conj(row_r)^H . (Op z_col)
-            (op == 0 ? GA : GB)[(size_t)(rb2 * k + r) * m + col] = std::complex<double>(v.x, v.y);
+            const double2 v = hG[((size_t)c * na + a) * k + r];  // z_row^H (Op z_col)
+            (op == 0 ? GA : GB)[(size_t)(rb2 * k + r) * m + col] = cd(v.x, v.y);
           }
         }
-    for (int i = 0; i < m; ++i)  // Hermitian parts
+    for (int i = 0; i < m; ++i) {  // Hermitian parts
       for (int j = 0; j < i; ++j) {
-        const auto ga = 0.5 * (GA[(size_t)i * m + j] + std::conj(GA[(size_t)j * m + i]));
+        const cd ga = 0.5 * (GA[(size_t)i * m + j] + std::conj(GA[(size_t)j * m + i]));
         GA[(size_t)i * m + j] = ga;
         GA[(size_t)j * m + i] = std::conj(ga);
-        const auto gb = 0.5 * (GB[(size_t)i * m + j] + std::conj(GB[(size_t)j * m + i]));
+        const cd gb = 0.5 * (GB[(size_t)i * m + j] + std::conj(GB[(size_t)j * m + i]));
         GB[(size_t)i * m + j] = gb;
         GB[(size_t)j * m + i] = std::conj(gb);
       }
-    for (int i = 0; i < m; ++i) {
       GA[(size_t)i * m + i] = GA[(size_t)i * m + i].real();
       GB[(size_t)i * m + i] = GB[(size_t)i * m + i].real();
     }
+    // canonical orthogonalisation: GB = V diag(d) V^H, T = V_keep diag(d_keep)^{-1/2}
+    std::vector<double> d;
+    std::vector<cd> V;
+    jacobi_eig_herm(GB, m, d, V);
+    const double dmax = *std::max_element(d.begin(), d.end());
+    std::vector<int> keep;
+    for (int j = 0; j < m; ++j)
+      if (d[j] > 1e-13 * dmax) keep.push_back(j);
+    const int q = (int)keep.size();
+    if (q < k) continue;  // degenerate basis: keep this instance's pairs as they are
+    std::vector<cd> T((size_t)m * q);  // column-major m x q
+    for (int c2 = 0; c2 < q; ++c2)
+      for (int i = 0; i < m; ++i) T[(size_t)c2 * m + i] = V[(size_t)keep[c2] * m + i] / std::sqrt(d[keep[c2]]);
+    std::vector<cd> H((size_t)q * q, cd(0.0));  // T^H GA T, row-major
+    for (int i = 0; i < q; ++i)
+      for (int j = 0; j < q; ++j) {
+        cd sum = 0.0;
+        for (int r = 0; r < m; ++r) {
+          cd t = 0.0;
+          for (int c2 = 0; c2 < m; ++c2) t += GA[(size_t)r * m + c2] * T[(size_t)j * m + c2];
+          sum += std::conj(T[(size_t)i * m + r]) * t;
+        }
+        H[(size_t)i * q + j] = sum;
+      }
+    for (int i = 0; i < q; ++i)
+      for (int j = 0; j < i; ++j) {
+        const cd h = 0.5 * (H[(size_t)i * q + j] + std::conj(H[(size_t)j * q + i]));
+        H[(size_t)i * q + j] = h;
+        H[(size_t)j * q + i] = std::conj(h);
+      }
     std::vector<double> mu;
-    std::vector<std::complex<double>> Yv;
-    if (!herm_pencil_eig(GA, GB, m, mu, Yv)) return fail(&P, FAME_ERR_BREAKDOWN, "refine: [X Y]^H B [X Y] not definite");
-    std::vector<int> ind(m);
+    std::vector<cd> Yv;
+    jacobi_eig_herm(H, q, mu, Yv);
+    std::vector<int> ind(q);
     std::iota(ind.begin(), ind.end(), 0);
     std::stable_sort(ind.begin(), ind.end(), [&](int x, int y) { return mu[x] > mu[y]; });
     for (int j = 0; j < k; ++j) {
       lam_new[(size_t)a * k + j] = mu[ind[j]];
-      for (int i = 0; i < m; ++i) {
-        const auto v = Yv[(size_t)ind[j] * m + i];
-        hC[((size_t)a * k + j) * m + i] = make_double2(v.real(), v.imag());  // column j of instance a (m x k)
+      for (int i = 0; i < m; ++i) {  // c = T y
+        cd v = 0.0;
+        for (int c2 = 0; c2 < q; ++c2) v += T[(size_t)c2 * m + i] * Yv[(size_t)ind[j] * q + c2];
+        hC[((size_t)a * k + j) * m + i] = make_double2(v.real(), v.imag());
       }
     }
   }
   FAME_CK(h2d_async(P, C, hC.data(), sizeof(double2) * hC.size()), "refine combine");
-  // X_a <- [X_a Y_a] C_a
+  // refined vectors Xn_a = [X_a W_a] C_a into Rv (instances whose basis was degenerate keep X_a)
   for (int a = 0; a < na; ++a) {
+    bool set = false;
+    for (int i = 0; i < m * k && !set; ++i) set = hC[(size_t)a * m * k + i].x != 0.0 || hC[(size_t)a * m * k + i].y != 0.0;
+    if (!set) {
+      FAME_CK(cudaMemcpyAsync(Rv + (size_t)a * vs, X + (size_t)a * vs, cb * k, cudaMemcpyDeviceToDevice, st),
+              "refine combine");
+      continue;
+    }
     FAME_CK(cudaMemcpyAsync(Z, X + (size_t)a * vs, cb * k, cudaMemcpyDeviceToDevice, st), "refine combine");
-    FAME_CK(cudaMemcpyAsync(Z + (size_t)k * L, Y + (size_t)a * vs, cb * k, cudaMemcpyDeviceToDevice, st),
+    FAME_CK(cudaMemcpyAsync(Z + (size_t)k * L, W + (size_t)a * vs, cb * k, cudaMemcpyDeviceToDevice, st),
             "refine combine");
-    FAME_CK(block_comb<double>(Z, X + (size_t)a * vs, L, L, m, k, C + (size_t)a * m * k, st), "refine combine");
+    FAME_CK(block_comb<double>(Z, Rv + (size_t)a * vs, L, L, m, k, C + (size_t)a * m * k, st), "refine combine");
   }
-  std::copy(lam_new.begin(), lam_new.end(), lam);
-  // residuals after
-  FAME_CK(launch_fncA<double>(P, X, AX, nv, ctx, st), "refine fncA");
-  FAME_CK(launch_fncB<double>(P, X, BX, nv, ctx, W0, W1, st), "refine fncB");
-  for (int i = 0; i < nv; ++i) b64_vec[i]++;
+  // residuals after (W, AW, BW reused as the refined vectors' A / B products)
+  FAME_CK(launch_fncA<double>(P, Rv, AW, nv, ctx, st), "refine fncA");
+  FAME_CK(launch_fncB<double>(P, Rv, BW, nv, ctx, W0, W1, st), "refine fncB");
+  for (int i = 0; i < nv; ++i) {
+    b64_vec[i]++;
+    mom[i] = -1.0 / lam_new[i];
+  }
   std::vector<double> ra(nv);
-  if ((rc = nfsep(AX, BX, lam, ra.data()))) return rc;
+  if ((rc = combine(AW, mom, BW, ones, W))) return rc;
+  if ((rc = norms(W, ra.data()))) return rc;
+  // keep the sweep's pair only where it lowered the residual
+  for (int i = 0; i < nv; ++i) {
+    if (ra[i] <= rb[i]) {
+      FAME_CK(cudaMemcpyAsync(X + (size_t)i * L, Rv + (size_t)i * L, cb, cudaMemcpyDeviceToDevice, st), "refine out");
+      lam[i] = lam_new[i];
+    } else {
+      ra[i] = rb[i];
+    }
+  }
   if (res_after) std::copy(ra.begin(), ra.end(), res_after);
+  FAME_CK(cudaStreamSynchronize(st), "refine out");
   return FAME_OK;
 }
 

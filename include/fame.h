@@ -95,11 +95,12 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *                     on either side of the target.
  *   FAME_OPT_REFINE   mixed form (FAME_C64) of fame_lanczos / fame_band_solve:
  *                     one FP64 refinement sweep of the converged Ritz pairs
- *                     [1]: Y = B^-1 A X by the mixed inner solve, then FP64
- *                     Rayleigh-Ritz on [X Y] per k-point; the returned
- *                     eigenvalues, vectors and residuals are the refined ones
- *                     (the residuals before: fame_refine_residuals).
- *   FAME_OPT_REFINE_TOL  inner B^-1 tolerance of that sweep [1e-12]. */
+ *                     [1]: W = B^-1 (A X - B X Lambda) by the mixed inner
+ *                     solve, then FP64 Rayleigh-Ritz on [X W] per k-point; the
+ *                     returned eigenvalues, vectors and residuals are the
+ *                     refined ones where the sweep lowered the residual (the
+ *                     residuals before: fame_refine_residuals).
+ *   FAME_OPT_REFINE_TOL  relative tolerance of that correction solve [1e-6]. */
 enum fame_option {
   FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2, FAME_OPT_ITOL_FLOOR = 3, FAME_OPT_PLANE_SPLIT = 4,
   FAME_OPT_SIRA_NEAREST = 5, FAME_OPT_REFINE = 6, FAME_OPT_REFINE_TOL = 7

@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import os
 import sys
+import time
 
 import numpy as np
 
@@ -117,10 +118,19 @@ def compute_n60_eig(k=10):
     P = O.build_problem(60, wave_vec=O.fcc_vertex("X"))
     L = 4 * 60 ** 3
     nits = []
-    _, ew, it = O.lanczos(P.A, P.B, lambda r: O.fncinvB(r, P.B, 1e-12, 10000, stats=nits), L, k, 1e-10, 10000,
+    nB = [0]
+
+    def fB(x):
+        nB[0] += 1
+        return P.B(x)
+
+    t0 = time.perf_counter()
+    _, ew, it = O.lanczos(P.A, fB, lambda r: O.fncinvB(r, fB, 1e-12, 10000, stats=nits), L, k, 1e-10, 10000,
                           2 * k, np.ones(L, complex))
     return {"ew": np.asarray(ew, dtype=np.float64), "theta": np.asarray(P.thetas, dtype=np.float64),
-            "lanczos_steps": np.array([it]), "pcg_iters": np.array([int(np.sum(nits))])}
+            "lanczos_steps": np.array([it]), "pcg_iters": np.array([int(np.sum(nits))]),
+            "b_applies": np.array([nB[0]]), "seconds": np.array([time.perf_counter() - t0]),
+            "cpu_threads": np.array([O.fft_workers()])}
 
 
 def images(A):

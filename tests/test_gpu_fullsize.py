@@ -1,8 +1,9 @@
 """Size-independent properties of the operators at the benchmark's full size
-(n = 60, where the oracle's sparse assembly is too slow to run in a test):
-the S-phased DFT is unitary and its 'transpose' inverts it, Prs / Qrs invert
-Pr / Qr, fncA and fncB are Hermitian, fncB is positive definite and linear,
-complex64 agrees with complex128, and fncinvB inverts fncB."""
+(n = 60; the operators' values there are held to the oracle by
+test_gpu_n60.py): the S-phased DFT is unitary and its 'transpose' inverts
+it, Prs / Qrs invert Pr / Qr, fncA and fncB are Hermitian, fncB is positive
+definite and linear, complex64 agrees with complex128, and fncinvB inverts
+fncB."""
 import pytest
 import torch
 
