@@ -233,6 +233,9 @@ k_sweep(const cx<R>* __restrict__ uv, cx<R>* __restrict__ out, PlanData<R> d, co
   const cx<R>* tau = d.tau + inst * 3;
   const cx<R> Tx = tau[0], Ty = tau[1], Tz = tau[2];
   const cx<R> tx = cconj(Tx), ty = cconj(Ty), tz = cconj(Tz);
+  // products of two shifts' phases (diagonal neighbours), once per CTA
+  const cx<R> txty = cmul(tx, ty), txtz = cmul(tx, tz), tytz = cmul(ty, tz);
+  const cx<R> TxTy = cmul(Tx, Ty), TxTz = cmul(Tx, Tz), TyTz = cmul(Ty, Tz);
   const cx<R>* tab = d.fld ? nullptr : d.mat + inst * nphase * 27;
   const bool tab_sm = !d.fld && nphase <= SH::TAB_MAX;
   if (tab_sm)
@@ -264,6 +267,13 @@ k_sweep(const cx<R>* __restrict__ uv, cx<R>* __restrict__ out, PlanData<R> d, co
   };
 
   double acc = 0.0;  // sum of Re(conj(w) . out) over this CTA's outputs (wdot)
+  // Each thread evaluates stage 1 at the same (row, x) of every plane, so its
+  // vertex's phase id for the next plane is loaded one step ahead.
+  const int h_hr = tid / N, h_x = tid - (tid / N) * N;
+  const bool h_act = tid < HR * N;
+  const int h_row = (y0 + h_hr) % N;
+  int ph_next = 0;
+  if (!d.fld && h_act) ph_next = __ldg(phase + ((z0 + N) % N) * NN + h_row * N + h_x);
   stage(0);
   for (int s = 0; s <= TZ + 1; ++s) {
     __syncthreads();  // readers of the buffers refilled below are done
@@ -281,28 +291,28 @@ k_sweep(const cx<R>* __restrict__ uv, cx<R>* __restrict__ out, PlanData<R> d, co
       const cx<R>* Fp = Fb + ((s - 1) % 3) * SH::F_ELEMS;
       cx<R>* H = Hb + (s % 2) * SH::H_ELEMS;
       R* D = Db + (s % 2) * SH::H_ELEMS;
-      for (int it = tid; it < HR * N; it += TPB) {
-        const int hr = it / N;
-        const int x = it - hr * N;
+      if (h_act) {
+        const int hr = h_hr;
+        const int x = h_x;
         const int xm = x == 0 ? N - 1 : x - 1;
         const int rc = hr + 1, rm = hr;  // staged rows of y and y-1
         auto at = [&](const cx<R>* F, int f, int r, int xx) { return F[(f * FR + r) * N + xx]; };
         // U_j = 1/4 (I + T_a^H)(I + T_b^H) u_j ; (T^H g)(r) = conj(tau) g(r - e)
-        auto g4 = [&](cx<R> g00, cx<R> ga, cx<R> gb, cx<R> gab, cx<R> ta, cx<R> tb) {
+        auto g4 = [&](cx<R> g00, cx<R> ga, cx<R> gb, cx<R> gab, cx<R> ta, cx<R> tb, cx<R> tab2) {
           cx<R> s4 = g00;
           s4 = cfma(ta, ga, s4);
           s4 = cfma(tb, gb, s4);
-          s4 = cfma(cmul(ta, tb), gab, s4);
+          s4 = cfma(tab2, gab, s4);
           return cscale(s4, R(0.25));
         };
         cx<R> U[3], V[3];
-        U[0] = g4(at(Fc, 0, rc, x), at(Fc, 0, rm, x), at(Fp, 0, rc, x), at(Fp, 0, rm, x), ty, tz);
-        U[1] = g4(at(Fc, 1, rc, x), at(Fc, 1, rc, xm), at(Fp, 1, rc, x), at(Fp, 1, rc, xm), tx, tz);
-        U[2] = g4(at(Fc, 2, rc, x), at(Fc, 2, rc, xm), at(Fc, 2, rm, x), at(Fc, 2, rm, xm), tx, ty);
+        U[0] = g4(at(Fc, 0, rc, x), at(Fc, 0, rm, x), at(Fp, 0, rc, x), at(Fp, 0, rm, x), ty, tz, tytz);
+        U[1] = g4(at(Fc, 1, rc, x), at(Fc, 1, rc, xm), at(Fp, 1, rc, x), at(Fp, 1, rc, xm), tx, tz, txtz);
+        U[2] = g4(at(Fc, 2, rc, x), at(Fc, 2, rc, xm), at(Fc, 2, rm, x), at(Fc, 2, rm, xm), tx, ty, txty);
         V[0] = cscale(cfma(tx, at(Fc, 3, rc, xm), at(Fc, 3, rc, x)), R(0.5));
         V[1] = cscale(cfma(ty, at(Fc, 4, rm, x), at(Fc, 4, rc, x)), R(0.5));
         V[2] = cscale(cfma(tz, at(Fp, 5, rc, x), at(Fc, 5, rc, x)), R(0.5));
-        const int vidx = zc * NN + ((y0 + hr) % N) * N + x;
+        const int vidx = zc * NN + h_row * N + x;
         cx<R> hu[3], hv[3];
         R dg[6];
         if (d.fld) {  // field mode: Mh = b G, Nh = a G, J = -i g G
@@ -323,24 +333,33 @@ k_sweep(const cx<R>* __restrict__ uv, cx<R>* __restrict__ out, PlanData<R> d, co
             dg[3 + i] = a * d.gram[i * 4];
           }
         } else {
-          const cx<R>* T = tab + __ldg(phase + vidx) * 27;
+          const cx<R>* T = tab + ph_next * 27;
+          ph_next = __ldg(phase + ((zc + 1) % N) * NN + h_row * N + x);  // the next plane's id, one step ahead
           const cx<R>* Nh = T;
           const cx<R>* Mh = T + 9;
           const cx<R>* J = T + 18;
+          // Herm(N), Herm(M): the upper off-diagonal entries and their conjugates
+          const cx<R> m01 = Mh[1], m02 = Mh[2], m12 = Mh[5];
+          const cx<R> n01 = Nh[1], n02 = Nh[2], n12 = Nh[5];
+          cx<R> Jr[9];
 #pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            cx<R> su = zero<R>(), sv = zero<R>();
+          for (int i = 0; i < 9; ++i) Jr[i] = J[i];
+          // Hu_i = sum_{j!=i} Mh_ij U_j + sum_j conj(J_ji) V_j ; Hv_i = sum_{j!=i} Nh_ij V_j + sum_j J_ij U_j
+          hu[0] = cfma(m01, U[1], cmul(m02, U[2]));
+          hu[1] = cfmac(m01, U[0], cmul(m12, U[2]));
+          hu[2] = cfmac(m02, U[0], cmulc(m12, U[1]));
+          hv[0] = cfma(n01, V[1], cmul(n02, V[2]));
+          hv[1] = cfmac(n01, V[0], cmul(n12, V[2]));
+          hv[2] = cfmac(n02, V[0], cmulc(n12, V[1]));
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
-              if (j != i) {
-                su = cfma(Mh[i * 3 + j], U[j], su);
-                sv = cfma(Nh[i * 3 + j], V[j], sv);
-              }
-              su = cfmac(J[j * 3 + i], V[j], su);
-              sv = cfma(J[i * 3 + j], U[j], sv);
+              hu[i] = cfmac(Jr[j * 3 + i], V[j], hu[i]);
+              hv[i] = cfma(Jr[i * 3 + j], U[j], hv[i]);
             }
-            hu[i] = su;
-            hv[i] = sv;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
             dg[i] = Mh[i * 4].x;
             dg[3 + i] = Nh[i * 4].x;
           }
@@ -370,11 +389,11 @@ k_sweep(const cx<R>* __restrict__ uv, cx<R>* __restrict__ out, PlanData<R> d, co
         auto h = [&](const cx<R>* Hp, int f, int rr, int xx) { return Hp[(f * HR + rr) * N + xx]; };
         auto dd = [&](const R* Dp, int f, int rr, int xx) { return Dp[(f * HR + rr) * N + xx]; };
         // u'_i = m_i u_i + 1/4 (I+T_a)(I+T_b) Hu_i ; (T g)(r) = tau g(r + e)
-        auto s4 = [&](cx<R> g00, cx<R> ga, cx<R> gb, cx<R> gab, cx<R> ta, cx<R> tb) {
+        auto s4 = [&](cx<R> g00, cx<R> ga, cx<R> gb, cx<R> gab, cx<R> ta, cx<R> tb, cx<R> tab2) {
           cx<R> q = g00;
           q = cfma(ta, ga, q);
           q = cfma(tb, gb, q);
-          q = cfma(cmul(ta, tb), gab, q);
+          q = cfma(tab2, gab, q);
           return cscale(q, R(0.25));
         };
         const R m0 = R(0.25) * (dd(D0, 0, r, x) + dd(D0, 0, r + 1, x) + dd(D1, 0, r, x) + dd(D1, 0, r + 1, x));
@@ -386,11 +405,11 @@ k_sweep(const cx<R>* __restrict__ uv, cx<R>* __restrict__ out, PlanData<R> d, co
         const int fr = r + 1;
         cx<R> o[6];
         o[0] = cadd(cscale(F[(0 * FR + fr) * N + x], m0),
-                    s4(h(H0, 0, r, x), h(H0, 0, r + 1, x), h(H1, 0, r, x), h(H1, 0, r + 1, x), Ty, Tz));
+                    s4(h(H0, 0, r, x), h(H0, 0, r + 1, x), h(H1, 0, r, x), h(H1, 0, r + 1, x), Ty, Tz, TyTz));
         o[1] = cadd(cscale(F[(1 * FR + fr) * N + x], m1),
-                    s4(h(H0, 1, r, x), h(H0, 1, r, xp), h(H1, 1, r, x), h(H1, 1, r, xp), Tx, Tz));
+                    s4(h(H0, 1, r, x), h(H0, 1, r, xp), h(H1, 1, r, x), h(H1, 1, r, xp), Tx, Tz, TxTz));
         o[2] = cadd(cscale(F[(2 * FR + fr) * N + x], m2),
-                    s4(h(H0, 2, r, x), h(H0, 2, r, xp), h(H0, 2, r + 1, x), h(H0, 2, r + 1, xp), Tx, Ty));
+                    s4(h(H0, 2, r, x), h(H0, 2, r, xp), h(H0, 2, r + 1, x), h(H0, 2, r + 1, xp), Tx, Ty, TxTy));
         o[3] = cadd(cscale(F[(3 * FR + fr) * N + x], n0), cscale(cfma(Tx, h(H0, 3, r, xp), h(H0, 3, r, x)), R(0.5)));
         o[4] = cadd(cscale(F[(4 * FR + fr) * N + x], n1), cscale(cfma(Ty, h(H0, 4, r + 1, x), h(H0, 4, r, x)), R(0.5)));
         o[5] = cadd(cscale(F[(5 * FR + fr) * N + x], n2), cscale(cfma(Tz, h(H1, 5, r, x), h(H0, 5, r, x)), R(0.5)));
