@@ -166,6 +166,15 @@ int upload_tables(Plan& P) {
   if (e == cudaSuccess) e = cudaMemcpy(d.sxyz, sx.data(), sizeof(cx<R>) * sx.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(d.mat, mat.data(), sizeof(cx<R>) * mat.size(), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(&P, e, "plan tables upload");
+  // Pi table for complex128 only: there the transform kernels are bound by
+  // GB300's FP64 rate and reading Pi (96 B per voxel) beats evaluating it
+  // (617 -> 496 us per n = 60 fncB vector); the complex64 kernels are
+  // issue-bound with L2 traffic to spare, and the extra 48 B per voxel made
+  // them slower (298 -> 314 us per 10 vectors), so they evaluate Pi.
+  if (sizeof(R) == 8) {
+    e = build_pi_table<R>(P);
+    if (e != cudaSuccess) return cuda_fail(&P, e, "plan Pi table");
+  }
   return FAME_OK;
 }
 
@@ -175,6 +184,7 @@ template <class R> void free_tables(PlanData<R>& d) {
   cudaFree(d.sxyz);
   cudaFree(d.mat);
   cudaFree(d.pc);
+  cudaFree(d.pi);
   cudaFree(d.fld);
   d = PlanData<R>();
 }
@@ -341,6 +351,10 @@ int fame_set_option(fame_plan_t h, int option, double value) {
       return FAME_OK;
     case FAME_OPT_SIRA_NEAREST:
       P.opt_sira_nearest = value != 0.0;
+      return FAME_OK;
+    case FAME_OPT_PI_TABLE:
+      P.opt_pi_table = value != 0.0;
+      free_graphs(P);  // captured sequences hold the old kernel arguments
       return FAME_OK;
     case FAME_OPT_REFINE:
       P.opt_refine = value != 0.0;

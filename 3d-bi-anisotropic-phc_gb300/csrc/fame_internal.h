@@ -54,6 +54,7 @@ template <class R> struct PlanData {
   cx<R>* sxyz = nullptr; // [nk][3n]  S_sDFT per axis (the MtxVecMul_FFT phase)
   cx<R>* mat = nullptr;  // [nk][nphase][27]: Herm(N) | Herm(M) | J, row-major 3x3 each
   cx<R>* pc = nullptr;   // [nk][8][Nq] CG preconditioner: inverse 4x4 Hermitian blocks, diagonal packed (lazy)
+  cx<R>* pi = nullptr;   // [nk][Nq][6] Pi1 | Pi2 per frequency voxel (SVD_Matrix_curl.m:45-57); complex128 plans data only
   // Field mode (per-vertex isotropic chiral medium eps(r) I, mu = I,
   // xi = -zeta = i gamma(r) I): vertex tensors N = a G, M = b G, J = -i g G with
   // a = 1/(eps - gamma^2), b = eps a, g = gamma a and G = A^T A the lattice
@@ -83,6 +84,7 @@ struct Plan {
   int opt_graph = 1;                  // replay CG iterations from captured CUDA graphs
   double opt_itol_floor = 1e-13;      // mixed form: floor of the spread-scaled inner tolerance
   int opt_plane_split = 1;            // fncB plane kernels with several threads per pencil where compiled
+  int opt_pi_table = 1;               // complex128 fncB reads Pi from the plan's table (else evaluates it)
   int opt_sira_nearest = 0;           // SIRA Ritz choice: 0 'CL' (above the target), 1 nearest either side
   int opt_refine = 1;                 // mixed form: FP64 refinement sweep of the Ritz pairs
   double opt_refine_tol = 1e-6;       // relative tolerance of its correction solve B^{-1} R
@@ -145,6 +147,10 @@ void free_workspaces(Plan& P);
 cudaError_t ensure_work(Plan& P, size_t vecs);
 int fail(Plan* P, int code, const std::string& msg);
 int cuda_fail(Plan* P, cudaError_t e, const char* where);
+
+// Pi1 | Pi2 of every frequency voxel of every instance into d.pi (allocated
+// here; called once at plan creation, after the lambda tables are on the device).
+template <class R> cudaError_t build_pi_table(Plan& P);
 
 // ---- kernel launchers (fncb_kernels.cu) ----
 // pq (may be null): partial sums of Re(x^H B x), fncB_pq_partials(P, nvec)

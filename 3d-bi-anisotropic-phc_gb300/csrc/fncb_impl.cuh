@@ -77,6 +77,40 @@ __device__ __forceinline__ PiBlock<R> pi_block(cx<R> lx, cx<R> ly, cx<R> lz) {
   return P;
 }
 
+// Pi1 | Pi2 of one voxel from the plan's table (6 complex; three 16-byte
+// loads in complex64).
+template <class R>
+__device__ __forceinline__ PiBlock<R> pi_load(const cx<R>* p) {
+  PiBlock<R> P;
+  if constexpr (sizeof(R) == 4) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+    const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+    P.p1[0] = mk<R>(a.x, a.y);
+    P.p1[1] = mk<R>(a.z, a.w);
+    P.p1[2] = mk<R>(b.x, b.y);
+    P.p2[0] = mk<R>(b.z, b.w);
+    P.p2[1] = mk<R>(c.x, c.y);
+    P.p2[2] = mk<R>(c.z, c.w);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      P.p1[i] = __ldg(p + i);
+      P.p2[i] = __ldg(p + 3 + i);
+    }
+  }
+  P.sig = R(0);
+  return P;
+}
+
+// Pi of voxel (i1, i2, k3) of instance inst: from the table when the plan has
+// one (voxel index k3*N*N + e, e = i2*N + i1), else evaluated.
+template <class R, int N>
+__device__ __forceinline__ PiBlock<R> pi_at(const PlanData<R>& d, int inst, int k3, int e, const cx<R>* lam, int i1,
+                                            int i2, cx<R> lz) {
+  if (d.pi) return pi_load<R>(d.pi + ((size_t)inst * N * N * N + (size_t)k3 * N * N + e) * 6);
+  return pi_block<R>(lam[i1], lam[N + i2], lz);
+}
+
 template <class R> __device__ __forceinline__ R rsqrt_n3(int n) {
   return R(1) / sqrt(R(n) * R(n) * R(n));
 }
@@ -133,7 +167,7 @@ k_plane_inv(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d,
         const int i2 = e / N, i1 = e - i2 * N;
         cx<R> v0, v1, v2;
         if constexpr (PREP) {
-          PiBlock<R> P = pi_block<R>(lam[i1], lam[N + i2], lam[2 * N + k3]);
+          PiBlock<R> P = pi_at<R, N>(d, inst, k3, e, lam, i1, i2, lam[2 * N + k3]);
           const cx<R> a = in[it][0], b = in[it][1];
           if (side == 0) {
             v0 = cfmac(P.p1[0], b, cneg(cmulc(P.p2[0], a)));
@@ -249,7 +283,7 @@ k_plane_fwd(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, V
     cx<R> u1 = sm[(1 * N + i2) * LD + i1];
     cx<R> u2 = sm[(2 * N + i2) * LD + i1];
     if constexpr (POST) {
-      PiBlock<R> P = pi_block<R>(lam[i1], lam[N + i2], lam[2 * N + k3]);
+      PiBlock<R> P = pi_at<R, N>(d, inst, k3, e, lam, i1, i2, lam[2 * N + k3]);
       cx<R> a, b;
       if (side == 0) {
         a = cneg(cfma(P.p2[2], u2, cfma(P.p2[1], u1, cmul(P.p2[0], u0))));
@@ -377,7 +411,7 @@ k_plane_inv2(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d
       const int e = tid + it * T;
       if (tid < T && e < N * N) {
         const int i2 = e / N, i1 = e - i2 * N;
-        PiBlock<R> P = pi_block<R>(lam[i1], lam[N + i2], lz);
+        PiBlock<R> P = pi_at<R, N>(d, inst, k3, e, lam, i1, i2, lz);
         const cx<R> a = cscale(in[it][0], sc), b = cscale(in[it][1], sc);
         cx<R> v0, v1, v2;
         if (side == 0) {
@@ -503,7 +537,7 @@ k_plane_fwd2(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, 
     const cx<R> u0 = sm[(0 * N + i2) * LD + i1];
     const cx<R> u1 = sm[(1 * N + i2) * LD + i1];
     const cx<R> u2 = sm[(2 * N + i2) * LD + i1];
-    PiBlock<R> P = pi_block<R>(lam[i1], lam[N + i2], lz);
+    PiBlock<R> P = pi_at<R, N>(d, inst, k3, e, lam, i1, i2, lz);
     cx<R> a, b;
     if (side == 0) {
       a = cneg(cfma(P.p2[2], u2, cfma(P.p2[1], u1, cmul(P.p2[0], u0))));
@@ -627,7 +661,8 @@ cudaError_t col(const PlanData<R>& d, cx<R>* w, int nfield, int nvec, long long 
 template <class R, int N>
 cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx, cx<R>* w0, cx<R>* w1,
                    cudaStream_t st, double2* pq) {
-  const PlanData<R>& d = pdata<R>(P);
+  PlanData<R> d = pdata<R>(P);
+  if (!P.opt_pi_table) d.pi = nullptr;  // evaluate Pi in the plane kernels instead
   const long long Nq = P.Nq;
   const TuneEntry tn = tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec);
   const int chunk = (tn.chunk > 0 && tn.chunk < nvec) ? tn.chunk : nvec;

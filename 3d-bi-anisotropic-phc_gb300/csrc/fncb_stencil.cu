@@ -48,6 +48,24 @@ __global__ void k_fncA(const cx<R>* __restrict__ x, cx<R>* __restrict__ y, PlanD
   yv[3 * Nq] = cscale(cmul_i<-1>(b1), inv);
 }
 
+// Pi1 | Pi2 per frequency voxel of each instance (SVD_Matrix_curl.m:45-57),
+// the same pi_block the transform kernels would evaluate.
+template <class R>
+__global__ void k_pi_table(const cx<R>* __restrict__ lam_all, int n, long long Nq, cx<R>* __restrict__ out) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int inst = blockIdx.y;
+  if (idx >= Nq) return;
+  const int i1 = int(idx % n), i2 = int((idx / n) % n), i3 = int(idx / ((long long)n * n));
+  const cx<R>* lam = lam_all + (long long)inst * 3 * n;
+  const PiBlock<R> P = pi_block<R>(lam[i1], lam[n + i2], lam[2 * n + i3]);
+  cx<R>* o = out + ((long long)inst * Nq + idx) * 6;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    o[i] = P.p1[i];
+    o[3 + i] = P.p2[i];
+  }
+}
+
 inline dim3 grid_pts1(long long Nq, int nvec, int tpb) {
   return dim3((unsigned)((Nq + tpb - 1) / tpb), (unsigned)nvec, 1);
 }
@@ -76,6 +94,24 @@ template cudaError_t stencil<double>(const Plan&, cx<double>*, cx<double>*, int,
 
 }  // namespace detail
 using namespace detail;
+
+template <class R>
+cudaError_t build_pi_table(Plan& P) {
+  PlanData<R>& d = const_cast<PlanData<R>&>(pdata<R>(P));
+  if (d.pi) return cudaSuccess;
+  cudaError_t e = cudaMalloc(&d.pi, sizeof(cx<R>) * 6 * (size_t)P.Nq * P.nk);
+  if (e != cudaSuccess) {
+    d.pi = nullptr;
+    return e;
+  }
+  FAME_LAUNCHED(1);
+  k_pi_table<R><<<dim3((unsigned)((P.Nq + 255) / 256), (unsigned)P.nk), 256, 0, P.stream>>>(d.lam, P.n, P.Nq, d.pi);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(P.stream);
+  return e;
+}
+template cudaError_t build_pi_table<float>(Plan&);
+template cudaError_t build_pi_table<double>(Plan&);
 
 // Partials per vector that fncB's pq output receives for a batch of nvec, or
 // 0 when the tuned form of that batch does not produce them.

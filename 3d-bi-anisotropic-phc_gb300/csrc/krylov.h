@@ -33,6 +33,10 @@ cudaError_t cg_scalars(int stage, int nvec, const double2* dot, double* rho, dou
 cudaError_t cg_scalars_red(int stage, int nvec, const double2* partial, int nblk, double2* dot, double* rho,
                            double* alpha, double* beta, const double* tol2b2, int* active, int* iters, double* res2,
                            cudaStream_t st);
+// r -= sum_i c_i X[:, i] with the correction evaluated in FP32 from a complex64
+// copy X of the columns (m <= 128); for coefficients far below |r|.
+cudaError_t sub_combo_lo(double2* r, const float2* X, long long len, long long ld, int m, const double2* c,
+                         cudaStream_t st);
 // partial[v * nblk + i] = block i's share of a_v^H b_v (no final reduction)
 template <class R>
 cudaError_t dot_partial(const cx<R>* a, const cx<R>* b, long long len, long long stride, int nvec, double2* partial,

@@ -318,6 +318,32 @@ __global__ void k_block_comb(const cx<R>* __restrict__ in, cx<R>* __restrict__ o
   }
 }
 
+// r -= sum_i c_i X[:, i] with X a complex64 copy: the correction is
+// evaluated in FP32 and subtracted from the FP64 r.  For Gram-Schmidt
+// coefficients far below |r| (a reorthogonalisation after the three-term
+// recurrence, |c| ~ 1e-10 |r|) the FP32 error of the correction,
+// ~6e-8 |c|, lies below FP64 rounding of r.
+__global__ void k_sub_combo_lo(double2* __restrict__ r, const float2* __restrict__ X, long long len, long long ld,
+                               int m, const double2* __restrict__ c) {
+  __shared__ float2 cs[128];
+  for (int i = threadIdx.x; i < m; i += blockDim.x) cs[i] = make_float2(float(c[i].x), float(c[i].y));
+  __syncthreads();
+  for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < len;
+       row += (long long)gridDim.x * blockDim.x) {
+    float ax = 0.f, ay = 0.f;
+    for (int i = 0; i < m; ++i) {
+      const float2 v = X[(long long)i * ld + row];
+      const float2 q = cs[i];
+      ax += q.x * v.x - q.y * v.y;
+      ay += q.x * v.y + q.y * v.x;
+    }
+    double2 o = r[row];
+    o.x -= double(ax);
+    o.y -= double(ay);
+    r[row] = o;
+  }
+}
+
 // r -= sum_i c_i X[:, i]  (complex coefficients, FP64)
 template <class R>
 __global__ void k_sub_combo(cx<R>* __restrict__ r, const cx<R>* __restrict__ X, long long len, long long ld, int m,
@@ -456,6 +482,15 @@ cudaError_t cg_xr_partial(cx<R>* x, cx<R>* r, const cx<R>* p, const cx<R>* q, lo
                           cudaStream_t st) {
   FAME_LAUNCHED(1);
   k_cg_xr_dot<R><<<dim3(nblk, nvec), kRedThreads, 0, st>>>(x, r, p, q, len, stride, alpha, active, partial);
+  return cudaGetLastError();
+}
+
+cudaError_t sub_combo_lo(double2* r, const float2* X, long long len, long long ld, int m, const double2* c,
+                         cudaStream_t st) {
+  if (m <= 0) return cudaSuccess;
+  if (m > 128) return cudaErrorInvalidValue;
+  FAME_LAUNCHED(1);
+  k_sub_combo_lo<<<grid_for(len), 256, 0, st>>>(r, X, len, ld, m, c);
   return cudaGetLastError();
 }
 

@@ -22,6 +22,7 @@ enum WsId {
   WS_MIX_B32, WS_MIX_X32, WS_MIX_RES, WS_MIX_MASK, WS_MIX_BD, WS_PCG_Z,
   WS_LZ_Q, WS_LZ_BQ, WS_LZ_VEC, WS_LZ_TMP, WS_LZ_COEF, WS_LZ_INST, WS_LZ_MASK, WS_LZ_U, WS_LZ_SCAL, WS_LZ_DOT,
   WS_LZ_PART,
+  WS_LZ_Q32 = 190, WS_LZ_BQ32,
   WS_RF_X = 200, WS_RF_AX, WS_RF_BX, WS_RF_Y, WS_RF_BY, WS_RF_AY, WS_RF_R, WS_RF_Z, WS_RF_INST, WS_RF_G, WS_RF_C,
   WS_RF_PART
 };
@@ -186,7 +187,8 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
                                        sizeof(R) == 4 ? (uintptr_t)P.d32.pc : (uintptr_t)P.d64.pc,
                                        (uintptr_t)tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).chunk,
                                        (uintptr_t)tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).stencil_tpb,
-                                       (uintptr_t)nblk_pq, (uintptr_t)P.opt_plane_split};
+                                       (uintptr_t)nblk_pq, (uintptr_t)P.opt_plane_split,
+                                       (uintptr_t)P.opt_pi_table};
   bool use_graph = P.opt_graph != 0;
   bool any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
   for (int it = 1; it <= maxit && any; it += chk) {
@@ -713,6 +715,39 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
   };
   const bool mixed = prec == FAME_C64;
   long long total_b = 0;
+  // Mixed form: complex64 copies of Q and B*Q for the corrections of the full
+  // Gram-Schmidt passes (Lanczos.m:69), whose coefficients are computed in
+  // FP64 against the FP64 columns and are ~1e-10 of |r|; the correction
+  // sum_i c_i q_i then needs only FP32 (section "reorthogonalisation" below).
+  // GB300's FP64 rate makes those column sums the cost of the pass.
+  float2* Q32 = nullptr;
+  float2* BQ32 = nullptr;
+  if (mixed) {
+    Q32 = (float2*)workspace(P, WS_LZ_Q32, sizeof(float2) * L * p * na, &e);
+    FAME_CK(e, "lanczos workspace Q32");
+    BQ32 = (float2*)workspace(P, WS_LZ_BQ32, sizeof(float2) * L * p * na, &e);
+    FAME_CK(e, "lanczos workspace BQ32");
+  }
+  auto copy_lo = [&](int a, int col0, int m) -> int {  // Q32, BQ32 columns col0 .. col0+m-1 of instance a
+    if (!mixed || m <= 0) return FAME_OK;
+    const size_t o = ((size_t)a * p + col0) * L;
+    FAME_CK((convert<float, double>(Q + o, Q32 + o, L * m, st)), "lanczos lo copy");
+    FAME_CK((convert<float, double>(BQ + o, BQ32 + o, L * m, st)), "lanczos lo copy");
+    return FAME_OK;
+  };
+  // reorthogonalisation against columns col0 .. col0+m-1: FP64 coefficients,
+  // corrections from the complex64 copies
+  auto project_out_lo = [&](int a, double2* r, double2* br, int col0, int m) -> int {
+    const double2* BQa = BQ + (size_t)a * p * L;
+    const float2* Q32a = Q32 + (size_t)a * p * L;
+    const float2* BQ32a = BQ32 + (size_t)a * p * L;
+    double2* ca = coef + (size_t)a * 128;
+    FAME_CK(dot_batched<double>(BQa + (size_t)col0 * L, 0, L, m, r, 0, L, 1, ca, part, nblk1, nullptr, st),
+            "lanczos gs dot");
+    FAME_CK(sub_combo_lo(r, Q32a + (size_t)col0 * L, L, L, m, ca, st), "lanczos gs");
+    if (br) FAME_CK(sub_combo_lo(br, BQ32a + (size_t)col0 * L, L, L, m, ca, st), "lanczos gs");
+    return FAME_OK;
+  };
 
   // v0 (Lanczos.m:8; band_structure...:78-80): ones, or the caller's vector
   {
@@ -771,6 +806,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
       const int j = S[a].j - 1;
       FAME_CK(cudaMemcpyAsync(Q + ((size_t)a * p + j) * L, V + (size_t)a * L, cb, cudaMemcpyDeviceToDevice, st), "lz");
       FAME_CK(cudaMemcpyAsync(BQ + ((size_t)a * p + j) * L, BV + (size_t)a * L, cb, cudaMemcpyDeviceToDevice, st), "lz");
+      if (int rc2 = copy_lo(a, j, 1)) return rc2;
     }
     // r = fncA(q); alpha = real(r'*q)   (Lanczos.m:50-51)
     FAME_CK(launch_fncA<double>(P, V, AQ, na, ctx, st), "lanczos fncA");
@@ -831,7 +867,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
       if (mixed)  // ||r||_B^2 before the full pass, next to the pass's coefficients
         FAME_CK(dot_batched<double>(r, 0, L, 1, br, 0, L, 1, coef + (size_t)a * 128 + 127, part, nblk1, nullptr, st),
                 "lanczos norm");
-      if ((rc = project_out(a, r, br, 0, I.j))) return rc;  // :69, first pass
+      if ((rc = mixed ? project_out_lo(a, r, br, 0, I.j) : project_out(a, r, br, 0, I.j))) return rc;  // :69
       second[a] = 1;
       I.steps++;
     }
@@ -850,7 +886,9 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     }
     for (int a = 0; a < na; ++a)
       if (second[a] && !S[a].done)
-        if ((rc = project_out(a, PR + (size_t)a * L, mixed ? BPR + (size_t)a * L : nullptr, 0, S[a].j))) return rc;
+        if ((rc = mixed ? project_out_lo(a, PR + (size_t)a * L, BPR + (size_t)a * L, 0, S[a].j)
+                        : project_out(a, PR + (size_t)a * L, nullptr, 0, S[a].j)))
+          return rc;
     prof.mark(2);
     // rr = fncB(r); beta = sqrt(r'*rr); v = r/beta  (Lanczos.m:72-74)
     if (!mixed) {
@@ -986,6 +1024,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         I.bapplies += k;
         I.refresh_bq = false;
       }
+      if (int rc2 = copy_lo(a, 0, k)) return rc2;
       FAME_CK(cudaStreamSynchronize(st), "lz restart");
       I.k = k;
       I.justRestarted = true;

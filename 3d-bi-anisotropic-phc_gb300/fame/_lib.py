@@ -33,6 +33,7 @@ FAME_OPT_PLANE_SPLIT = 4
 FAME_OPT_SIRA_NEAREST = 5
 FAME_OPT_REFINE = 6
 FAME_OPT_REFINE_TOL = 7
+FAME_OPT_PI_TABLE = 8
 FAME_SHAPE_WOODPILE, FAME_SHAPE_SPHERE, FAME_SHAPE_TETRA = 0, 1, 2
 FAME_RASTER_PAINT = 2
 

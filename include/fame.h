@@ -100,10 +100,14 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *                     returned eigenvalues, vectors and residuals are the
  *                     refined ones where the sweep lowered the residual (the
  *                     residuals before: fame_refine_residuals).
- *   FAME_OPT_REFINE_TOL  relative tolerance of that correction solve [1e-6]. */
+ *   FAME_OPT_REFINE_TOL  relative tolerance of that correction solve [1e-6].
+ *   FAME_OPT_PI_TABLE  complex128 fncB reads the per-voxel Pi blocks from the
+ *                     table the plan builds at creation (96 B per voxel and
+ *                     k-point) [1]; 0 evaluates them in the transform kernels
+ *                     (same values to rounding).  Complex64 always evaluates. */
 enum fame_option {
   FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2, FAME_OPT_ITOL_FLOOR = 3, FAME_OPT_PLANE_SPLIT = 4,
-  FAME_OPT_SIRA_NEAREST = 5, FAME_OPT_REFINE = 6, FAME_OPT_REFINE_TOL = 7
+  FAME_OPT_SIRA_NEAREST = 5, FAME_OPT_REFINE = 6, FAME_OPT_REFINE_TOL = 7, FAME_OPT_PI_TABLE = 8
 };
 int fame_set_option(fame_plan_t plan, int option, double value);
 
