@@ -154,10 +154,12 @@ template <class R> cudaError_t build_pi_table(Plan& P);
 
 // ---- kernel launchers (fncb_kernels.cu) ----
 // pq (may be null): partial sums of Re(x^H B x), fncB_pq_partials(P, nvec)
-// per vector, written when that count is non-zero.
+// per vector, written when that count is non-zero.  pupd_z (may be null): x
+// is a CG direction that is first updated in place, x = pupd_z + pupd_beta[v] x.
 template <class R>
 cudaError_t launch_fncB(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,
-                        cx<R>* w0, cx<R>* w1, cudaStream_t st, double2* pq = nullptr);
+                        cx<R>* w0, cx<R>* w1, cudaStream_t st, double2* pq = nullptr,
+                        const cx<R>* pupd_z = nullptr, const double* pupd_beta = nullptr);
 template <class R> int fncB_pq_partials(const Plan& P, int nvec);
 template <class R>
 cudaError_t launch_fncA(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,

@@ -115,6 +115,14 @@ template <class R> __device__ __forceinline__ R rsqrt_n3(int n) {
   return R(1) / sqrt(R(n) * R(n) * R(n));
 }
 
+// The conjugate-gradient direction update p = z + beta p, done by the first
+// kernel of fncB on the p it reads (z == null: no update).  Each CTA rewrites
+// the plane of p it loads, so the separate update pass over p disappears.
+template <class R> struct DirUpd {
+  const cx<R>* z = nullptr;     // same layout and strides as p
+  const double* beta = nullptr; // [nvec] of this launch
+};
+
 // ---------------------------------------------------------------------------
 // plane_inv: one CTA per (k3 plane, side, vector); 3N threads.
 // PREP: build the 3 frequency components of one side from (a, b):
@@ -127,7 +135,7 @@ template <class R> __device__ __forceinline__ R rsqrt_n3(int n) {
 template <class R, int N, bool PREP, bool WITH_S>
 __global__ void __launch_bounds__(((3 * N + 31) / 32) * 32, sizeof(R) == 4 ? 2 : 1)
 k_plane_inv(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d, VecCtx ctx,
-            long long in_stride, long long in_side_stride, long long out_stride, int side0) {
+            long long in_stride, long long in_side_stride, long long out_stride, int side0, DirUpd<R> upd) {
   constexpr int LD = N + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);  // [3][N][LD]
@@ -158,6 +166,24 @@ k_plane_inv(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d,
       if (base + it < ITEMS && e < N * N) {
 #pragma unroll
         for (int c = 0; c < NB; ++c) in[it][c] = xin[c * Nq + e];
+      }
+    }
+    if (PREP && upd.z) {  // p = z + beta p, written back
+      const long long off = vec * in_stride + blockIdx.y * in_side_stride + (long long)k3 * N * N;
+      const cx<R>* zin = upd.z + off;
+      cx<R>* xw = const_cast<cx<R>*>(x) + off;
+      const R bt = R(upd.beta[vec]);
+#pragma unroll
+      for (int it = 0; it < PF; ++it) {
+        const int e = tid + (base + it) * T;
+        if (base + it < ITEMS && e < N * N) {
+#pragma unroll
+          for (int c = 0; c < NB; ++c) {
+            const cx<R> zz = zin[c * Nq + e];
+            in[it][c] = mk<R>(zz.x + bt * in[it][c].x, zz.y + bt * in[it][c].y);
+            xw[c * Nq + e] = in[it][c];
+          }
+        }
       }
     }
 #pragma unroll
@@ -376,7 +402,7 @@ template <int G, class F> __device__ __forceinline__ void with_g(int g, F&& f) {
 template <class R, int N, bool PREP_UNUSED = true>
 __global__ void __launch_bounds__(Split<N, plane_split(N)>::TB, sizeof(R) == 4 ? 2 : 1)
 k_plane_inv2(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d, VecCtx ctx,
-             long long in_stride, long long in_side_stride, long long out_stride, int side0) {
+             long long in_stride, long long in_side_stride, long long out_stride, int side0, DirUpd<R> upd) {
   constexpr int G = plane_split(N);
   using SP = Split<N, G>;
   constexpr int M = SP::M, T = SP::T, LD = N + 1;
@@ -402,6 +428,24 @@ k_plane_inv2(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d
       if (tid < T && e < N * N) {
         in[it][0] = xin[e];
         in[it][1] = xin[Nq + e];
+      }
+    }
+    if (upd.z) {  // p = z + beta p, written back
+      const long long off = vec * in_stride + blockIdx.y * in_side_stride + (long long)k3 * N * N;
+      const cx<R>* zin = upd.z + off;
+      cx<R>* xw = const_cast<cx<R>*>(x) + off;
+      const R bt = R(upd.beta[vec]);
+#pragma unroll
+      for (int it = 0; it < ITEMS; ++it) {
+        const int e = tid + it * T;
+        if (tid < T && e < N * N) {
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            const cx<R> zz = zin[c * Nq + e];
+            in[it][c] = mk<R>(zz.x + bt * in[it][c].x, zz.y + bt * in[it][c].y);
+            xw[c * Nq + e] = in[it][c];
+          }
+        }
       }
     }
     const R sc = R(1) / R(N);
@@ -590,7 +634,7 @@ inline dim3 grid_pts(long long Nq, int nvec, int tpb) {
 template <class R, int N, bool PREP, bool WITH_S>
 cudaError_t plane_inv(const Plan& P, const PlanData<R>& d, const cx<R>* x, cx<R>* out, int nvec,
                       int nside, int side0, long long in_stride, long long in_side_stride,
-                      long long out_stride, const VecCtx& ctx, cudaStream_t st) {
+                      long long out_stride, const VecCtx& ctx, cudaStream_t st, DirUpd<R> upd = DirUpd<R>()) {
   const size_t sm = sizeof(cx<R>) * 3 * N * (N + 1);
   if constexpr (PREP && !WITH_S && plane_split(N) > 0) {
     if (P.opt_plane_split) {
@@ -599,7 +643,7 @@ cudaError_t plane_inv(const Plan& P, const PlanData<R>& d, const cx<R>* x, cx<R>
       if (e != cudaSuccess) return e;
       FAME_LAUNCHED(1);
       kfn<<<dim3(N, nside, nvec), Split<N, plane_split(N)>::TB, sm, st>>>(x, out, d, ctx, in_stride, in_side_stride,
-                                                                           out_stride, side0);
+                                                                           out_stride, side0, upd);
       return cudaGetLastError();
     }
   }
@@ -609,7 +653,7 @@ cudaError_t plane_inv(const Plan& P, const PlanData<R>& d, const cx<R>* x, cx<R>
   if (e != cudaSuccess) return e;
   FAME_LAUNCHED(1);
   kfn<<<dim3(N, nside, nvec), threads, sm, st>>>(x, out, d, ctx, in_stride, in_side_stride, out_stride,
-                                                 side0);
+                                                 side0, upd);
   return cudaGetLastError();
 }
 
@@ -658,9 +702,12 @@ cudaError_t col(const PlanData<R>& d, cx<R>* w, int nfield, int nvec, long long 
 // transforms are unitary and Pi has orthonormal columns, so x^H B x equals
 // w^H [M J^H; J N] w for the spatial fields w the stencil reads; the stencil
 // pass accumulates it while it writes its output.
+//
+// pupd_z / pupd_beta (may be null): x is a CG direction p, updated first as
+// p = z + beta p (in place) by the plane kernel that reads it.
 template <class R, int N>
 cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx, cx<R>* w0, cx<R>* w1,
-                   cudaStream_t st, double2* pq) {
+                   cudaStream_t st, double2* pq, const cx<R>* pupd_z, const double* pupd_beta) {
   PlanData<R> d = pdata<R>(P);
   if (!P.opt_pi_table) d.pi = nullptr;  // evaluate Pi in the plane kernels instead
   const long long Nq = P.Nq;
@@ -672,7 +719,12 @@ cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecC
     const cx<R>* xs = x + (size_t)v0 * 4 * Nq;
     cx<R>* ys = y + (size_t)v0 * 4 * Nq;
     cudaError_t e;
-    e = plane_inv<R, N, true, false>(P, d, xs, w0, nv, 2, 0, 4 * Nq, 2 * Nq, 6 * Nq, c, st);
+    DirUpd<R> upd;
+    if (pupd_z) {
+      upd.z = pupd_z + (size_t)v0 * 4 * Nq;
+      upd.beta = pupd_beta + v0;
+    }
+    e = plane_inv<R, N, true, false>(P, d, xs, w0, nv, 2, 0, 4 * Nq, 2 * Nq, 6 * Nq, c, st, upd);
     if (e != cudaSuccess) return e;
     e = col<R, N, +1, 0>(d, w0, 6, nv, 6 * Nq, c, st);
     if (e != cudaSuccess) return e;
@@ -751,7 +803,7 @@ cudaError_t handle_n(const Plan& P, int which, const cx<R>* x, cx<R>* y, int nve
 // suppress instantiation in other translation units).
 #define FAME_SIZE_SIGS(PFX, R, NN)                                                                                 \
   PFX cudaError_t fame::detail::fncB_n<R, NN>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&, cx<R>*,       \
-                                              cx<R>*, cudaStream_t, double2*);                                     \
+                                              cx<R>*, cudaStream_t, double2*, const cx<R>*, const double*);       \
   PFX cudaError_t fame::detail::stencil_n<R, NN>(const Plan&, cx<R>*, cx<R>*, int, const VecCtx&, cudaStream_t,    \
                                                  int);                                                             \
   PFX cudaError_t fame::detail::fields_inv_n<R, NN>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&,         \

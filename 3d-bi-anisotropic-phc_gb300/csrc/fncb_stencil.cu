@@ -137,10 +137,10 @@ bool n_supported(int n) {
 
 template <class R>
 cudaError_t launch_fncB(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx, cx<R>* w0,
-                        cx<R>* w1, cudaStream_t st, double2* pq) {
+                        cx<R>* w1, cudaStream_t st, double2* pq, const cx<R>* pupd_z, const double* pupd_beta) {
   if (nvec <= 0) return cudaSuccess;
   switch (P.n) {
-#define FAME_CASE(NN) case NN: return fncB_n<R, NN>(P, x, y, nvec, ctx, w0, w1, st, pq);
+#define FAME_CASE(NN) case NN: return fncB_n<R, NN>(P, x, y, nvec, ctx, w0, w1, st, pq, pupd_z, pupd_beta);
     FAME_FOR_EACH_N(FAME_CASE)
 #undef FAME_CASE
     default: return cudaErrorInvalidValue;
@@ -220,7 +220,7 @@ cudaError_t launch_material(const Plan& P, const cx<R>* uv, cx<R>* out, int nvec
 
 #define FAME_INST(R)                                                                                      \
   template cudaError_t launch_fncB<R>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&, cx<R>*,     \
-                                      cx<R>*, cudaStream_t, double2*);                                    \
+                                      cx<R>*, cudaStream_t, double2*, const cx<R>*, const double*);       \
   template int fncB_pq_partials<R>(const Plan&, int);                                                     \
   template cudaError_t launch_fncA<R>(const Plan&, const cx<R>*, cx<R>*, int, const VecCtx&,             \
                                       cudaStream_t);                                                      \

@@ -120,6 +120,8 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
     }
   }
   std::vector<int> it0(nvec, 0);
+  const std::vector<double> zero_beta(nvec, 0.0);  // the first direction is z itself
+  FAME_CK(h2d_async(P, S.beta, zero_beta.data(), sizeof(double) * nvec), "pcg init");
   FAME_CK(h2d_async(P, S.rho, rho.data(), sizeof(double) * nvec), "pcg init");
   FAME_CK(h2d_async(P, S.tol2b2, t2.data(), sizeof(double) * nvec), "pcg init");
   FAME_CK(h2d_async(P, S.res2, rho.data(), sizeof(double) * nvec), "pcg init");
@@ -143,7 +145,8 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
     z = (cx<R>*)workspace(P, WS_PCG_Z + (sizeof(R) == 4 ? 100 : 0), vb, &e);
     FAME_CK(e, "pcg workspace");
     FAME_CK(build_precond<R>(P, st), "pcg preconditioner");
-    FAME_CK(precond_apply<R>(P, b, p, nvec, ctx, part, nblkv, st), "pcg precond");
+    FAME_CK(precond_apply<R>(P, b, z, nvec, ctx, part, nblkv, st), "pcg precond");
+    FAME_CK(cudaMemcpyAsync(p, z, vb, cudaMemcpyDeviceToDevice, st), "pcg init");
     FAME_CK(dot_final(part, nblkv, nvec, S.dot, st), "pcg precond");
     std::vector<double2> rz(nvec);
     FAME_CK(cudaMemcpyAsync(rz.data(), S.dot, sizeof(double2) * nvec, cudaMemcpyDeviceToHost, st), "pcg init");
@@ -157,13 +160,15 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
   // One CG iteration: every kernel reads its scalars and active flags from
   // the device, so a block of iterations is a fixed launch sequence that is
   // captured once per (sizes, pointers) and replayed from a CUDA graph.
-  //   q = B p (with the partials of p^H q when the stencil pass provides them)
-  //   alpha = rho / p^H q            (partials reduced in the same launch)
+  //   p = z + beta p, q = B p         (the update done by fncB's first kernel;
+  //                                     beta = 0 before the first iteration;
+  //                                     with the partials of p^H q when the
+  //                                     stencil pass provides them)
+  //   alpha = rho / p^H q             (partials reduced in the same launch)
   //   x += alpha p, r -= alpha q, z = M r, partials of (r^H z, |r|^2)
-  //   beta, rho, convergence         (partials reduced in the same launch)
-  //   p = z + beta p
+  //   beta, rho, convergence          (partials reduced in the same launch)
   auto iteration = [&](cudaStream_t cs) -> cudaError_t {
-    cudaError_t e2 = launch_fncB<R>(P, p, q, nvec, ctx, w0, w1, cs, nblk_pq ? part : nullptr);
+    cudaError_t e2 = launch_fncB<R>(P, p, q, nvec, ctx, w0, w1, cs, nblk_pq ? part : nullptr, pre ? z : r, S.beta);
     if (e2 == cudaSuccess && !nblk_pq) e2 = dot_partial<R>(p, q, L, L, nvec, part, nblk, S.active, cs);
     if (e2 == cudaSuccess)
       e2 = cg_scalars_red(0, nvec, part, nblk_pq ? nblk_pq : nblk, S.dot, S.rho, S.alpha, S.beta, S.tol2b2,
@@ -176,7 +181,6 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
     if (e2 == cudaSuccess)
       e2 = cg_scalars_red(1, nvec, part, pre ? nblkv : nblk, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active,
                           S.iters, S.res2, cs);
-    if (e2 == cudaSuccess) e2 = cg_p<R>(p, pre ? z : r, L, L, nvec, S.beta, S.active, cs);
     return e2;
   };
   const int chk = 4;
