@@ -794,6 +794,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     }
   } prof;
   prof.on = std::getenv("FAME_PROFILE") != nullptr;
+  long long n_first = 0, n_second = 0;  // full Gram-Schmidt passes (FAME_PROFILE report)
   prof.st = st;
   prof.start();
   while (true) {
@@ -873,6 +874,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
                 "lanczos norm");
       if ((rc = mixed ? project_out_lo(a, r, br, 0, I.j) : project_out(a, r, br, 0, I.j))) return rc;  // :69
       second[a] = 1;
+      n_first++;
       I.steps++;
     }
     if (mixed) {
@@ -886,6 +888,7 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
                                                hc[(size_t)a * 128 + i].y * hc[(size_t)a * 128 + i].y;
         const double r2 = hc[(size_t)a * 128 + 127].x;
         second[a] = !(c2 <= 0.5 * r2);
+        n_second += second[a];
       }
     }
     for (int a = 0; a < na; ++a)
@@ -1041,8 +1044,9 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
   }
   if (prof.on)
     std::fprintf(stderr,
-                 "[fame lanczos] instances %d: fncA+alpha %.3fs  B^-1 %.3fs  reorth %.3fs  beta %.3fs  restart %.3fs\n",
-                 na, prof.acc[0], prof.acc[1], prof.acc[2], prof.acc[3], prof.acc[4]);
+                 "[fame lanczos] instances %d: fncA+alpha %.3fs  B^-1 %.3fs  reorth %.3fs  beta %.3fs  restart %.3fs"
+                 "  (second GS passes %lld of %lld)\n",
+                 na, prof.acc[0], prof.acc[1], prof.acc[2], prof.acc[3], prof.acc[4], n_second, n_first);
   // Ritz vectors ev = Q*U(:, ind(1:k0)) (Lanczos.m:146-152) and outputs
   double2* EV = ev;
   for (int a = 0; a < na; ++a) {
