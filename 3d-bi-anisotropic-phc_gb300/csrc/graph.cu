@@ -5,6 +5,19 @@ namespace fame {
 
 constexpr size_t kMaxGraphs = 8;
 
+unsigned long long graph_kernel_nodes(cudaGraph_t g) {
+  size_t n = 0;
+  if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return 0;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return 0;
+  unsigned long long k = 0;
+  for (size_t i = 0; i < n; ++i) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
+
 cudaError_t graph_lookup(Plan& P, const std::vector<uintptr_t>& key, GraphEntry** out) {
   *out = nullptr;
   for (GraphEntry& g : P.graphs)

@@ -6,6 +6,7 @@
 namespace fame {
 
 cudaError_t graph_lookup(Plan& P, const std::vector<uintptr_t>& key, GraphEntry** out);
+unsigned long long graph_kernel_nodes(cudaGraph_t g);
 cudaError_t graph_store(Plan& P, const std::vector<uintptr_t>& key, cudaGraph_t g, unsigned long long captured,
                         GraphEntry** out);
 
@@ -19,14 +20,16 @@ cudaError_t graph_replay(Plan& P, const std::vector<uintptr_t>& key, F&& issue) 
       e = cudaStreamCreateWithFlags(&P.cap_stream, cudaStreamNonBlocking);
       if (e != cudaSuccess) return e;
     }
-    const unsigned long long before = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
     e = cudaStreamBeginCapture(P.cap_stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
     cudaError_t ie = issue(P.cap_stream);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(P.cap_stream, &g);
-    // the launches above were recorded, not run: count them when replayed
-    const unsigned long long captured = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED) - before;
+    // The launches above were recorded, not run (each added one to the
+    // counter and one kernel node to the graph): count them when replayed.
+    // The graph's own kernel nodes are counted, not the counter's change,
+    // which also holds other threads' launches on other plans.
+    const unsigned long long captured = g ? graph_kernel_nodes(g) : 0;
     __atomic_fetch_sub(&g_kernel_launches, captured, __ATOMIC_RELAXED);
     if (ie != cudaSuccess || e != cudaSuccess) {
       if (g) cudaGraphDestroy(g);

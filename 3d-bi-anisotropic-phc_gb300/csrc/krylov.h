@@ -33,10 +33,23 @@ cudaError_t cg_scalars(int stage, int nvec, const double2* dot, double* rho, dou
 cudaError_t cg_scalars_red(int stage, int nvec, const double2* partial, int nblk, double2* dot, double* rho,
                            double* alpha, double* beta, const double* tol2b2, int* active, int* iters, double* res2,
                            cudaStream_t st);
-// r -= sum_i c_i X[:, i] with the correction evaluated in FP32 from a complex64
-// copy X of the columns (m <= 128); for coefficients far below |r|.
-cudaError_t sub_combo_lo(double2* r, const float2* X, long long len, long long ld, int m, const double2* c,
-                         cudaStream_t st);
+// Gram-Schmidt over a batch of instances, one launch each for all of them:
+// vector v of r (stride rs) works against columns span[v].x ..
+// span[v].x + span[v].y - 1 of its block X + v*xs (columns len apart);
+// span[v].y = 0 skips it; span[v].y <= maxm <= 128.
+// coef[v*cstride + i] = X_v[col0_v + i]^H r_v (FP64); partial: nv*maxm*nblk.
+cudaError_t gs_dots(const double2* X, long long xs, const double2* r, long long rs, long long len, int nv,
+                    const int2* span, int maxm, double2* coef, int cstride, double2* partial, int nblk,
+                    cudaStream_t st);
+// Q_v[:, col[v]] = V_v and BQ_v[:, col[v]] = BV_v (+ complex64 copies when Q32
+// is given) for every v with col[v] >= 0; blocks xs apart, vectors len apart.
+cudaError_t gs_store(double2* Q, double2* BQ, float2* Q32, float2* BQ32, long long xs, const double2* V,
+                     const double2* BV, long long len, int nv, const int* col, cudaStream_t st);
+// r_v -= sum_i coef[v*cstride + i] X_v[col0_v + i], FP64 or from complex64 copies
+cudaError_t gs_combo(double2* r, long long rs, const double2* X, long long xs, long long len, int nv,
+                     const int2* span, const double2* coef, int cstride, cudaStream_t st);
+cudaError_t gs_combo_lo(double2* r, long long rs, const float2* X, long long xs, long long len, int nv,
+                        const int2* span, const double2* coef, int cstride, cudaStream_t st);
 // partial[v * nblk + i] = block i's share of a_v^H b_v (no final reduction)
 template <class R>
 cudaError_t dot_partial(const cx<R>* a, const cx<R>* b, long long len, long long stride, int nvec, double2* partial,

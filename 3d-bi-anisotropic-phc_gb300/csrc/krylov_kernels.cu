@@ -318,29 +318,85 @@ __global__ void k_block_comb(const cx<R>* __restrict__ in, cx<R>* __restrict__ o
   }
 }
 
-// r -= sum_i c_i X[:, i] with X a complex64 copy: the correction is
-// evaluated in FP32 and subtracted from the FP64 r.  For Gram-Schmidt
-// coefficients far below |r| (a reorthogonalisation after the three-term
-// recurrence, |c| ~ 1e-10 |r|) the FP32 error of the correction,
-// ~6e-8 |c|, lies below FP64 rounding of r.
-__global__ void k_sub_combo_lo(double2* __restrict__ r, const float2* __restrict__ X, long long len, long long ld,
-                               int m, const double2* __restrict__ c) {
-  __shared__ float2 cs[128];
-  for (int i = threadIdx.x; i < m; i += blockDim.x) cs[i] = make_float2(float(c[i].x), float(c[i].y));
+// ---------------------------------------------------------------------------
+// Gram-Schmidt over a batch of k-point instances in one launch each: vector v
+// works against its own columns col0_v .. col0_v + m_v - 1 (span[v] = (col0, m),
+// m = 0 skips it) of its block X + v * xs (columns len apart).
+// ---------------------------------------------------------------------------
+// partial[(v * maxm + i) * nblk + blk] = block's share of X_v[col0_v + i]^H r_v
+__global__ void __launch_bounds__(kRedThreads)
+k_gs_dot_partial(const double2* __restrict__ X, long long xs, const double2* __restrict__ r, long long rs,
+                 long long len, const int2* __restrict__ span, int maxm, double2* __restrict__ partial) {
+  const int v = blockIdx.y, i = blockIdx.z, nblk = gridDim.x;
+  const int2 sp = span[v];
+  if (i >= sp.y) return;
+  const double2* a = X + v * xs + (long long)(sp.x + i) * len;
+  const double2* b = r + v * rs;
+  double sx = 0.0, sy = 0.0;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < len; k += (long long)nblk * blockDim.x) {
+    const double2 x = a[k], y = b[k];
+    sx += x.x * y.x + x.y * y.y;
+    sy += x.x * y.y - x.y * y.x;
+  }
+  const double2 s = block_sum2(make_double2(sx, sy));
+  if (threadIdx.x == 0) partial[((long long)v * maxm + i) * nblk + blockIdx.x] = s;
+}
+
+// coef[v * cstride + i] = sum over blocks (i < m_v)
+__global__ void __launch_bounds__(kRedThreads)
+k_gs_dot_final(const double2* __restrict__ partial, int nblk, int maxm, const int2* __restrict__ span,
+               double2* __restrict__ coef, int cstride) {
+  const int v = blockIdx.x / maxm, i = blockIdx.x - v * maxm;
+  if (i >= span[v].y) return;
+  double2 s = make_double2(0.0, 0.0);
+  for (int t = threadIdx.x; t < nblk; t += blockDim.x) {
+    const double2 q = partial[((long long)v * maxm + i) * nblk + t];
+    s.x += q.x;
+    s.y += q.y;
+  }
+  s = block_sum2(s);
+  if (threadIdx.x == 0) coef[(long long)v * cstride + i] = s;
+}
+
+// r_v -= sum_i coef[v * cstride + i] X_v[col0_v + i]  (FP64, or from a complex64 copy when XL)
+template <class XT>
+__global__ void k_gs_combo(double2* __restrict__ r, long long rs, const XT* __restrict__ X, long long xs,
+                           long long len, const int2* __restrict__ span, const double2* __restrict__ coef,
+                           int cstride) {
+  __shared__ double2 cs[128];
+  const int v = blockIdx.y;
+  const int2 sp = span[v];
+  if (sp.y <= 0) return;
+  for (int i = threadIdx.x; i < sp.y; i += blockDim.x) cs[i] = coef[(long long)v * cstride + i];
   __syncthreads();
+  const XT* x = X + v * xs + (long long)sp.x * len;
+  double2* rv = r + v * rs;
   for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < len;
        row += (long long)gridDim.x * blockDim.x) {
-    float ax = 0.f, ay = 0.f;
-    for (int i = 0; i < m; ++i) {
-      const float2 v = X[(long long)i * ld + row];
-      const float2 q = cs[i];
-      ax += q.x * v.x - q.y * v.y;
-      ay += q.x * v.y + q.y * v.x;
+    if constexpr (sizeof(XT) == 8) {  // complex64 copy: the correction in FP32
+      float ax = 0.f, ay = 0.f;
+      for (int i = 0; i < sp.y; ++i) {
+        const XT q = x[(long long)i * len + row];
+        const float cx_ = float(cs[i].x), cy_ = float(cs[i].y);
+        ax += cx_ * q.x - cy_ * q.y;
+        ay += cx_ * q.y + cy_ * q.x;
+      }
+      double2 o = rv[row];
+      o.x -= double(ax);
+      o.y -= double(ay);
+      rv[row] = o;
+    } else {
+      double ax = 0.0, ay = 0.0;
+      for (int i = 0; i < sp.y; ++i) {
+        const XT q = x[(long long)i * len + row];
+        ax += cs[i].x * q.x - cs[i].y * q.y;
+        ay += cs[i].x * q.y + cs[i].y * q.x;
+      }
+      double2 o = rv[row];
+      o.x -= ax;
+      o.y -= ay;
+      rv[row] = o;
     }
-    double2 o = r[row];
-    o.x -= double(ax);
-    o.y -= double(ay);
-    r[row] = o;
   }
 }
 
@@ -485,12 +541,64 @@ cudaError_t cg_xr_partial(cx<R>* x, cx<R>* r, const cx<R>* p, const cx<R>* q, lo
   return cudaGetLastError();
 }
 
-cudaError_t sub_combo_lo(double2* r, const float2* X, long long len, long long ld, int m, const double2* c,
-                         cudaStream_t st) {
-  if (m <= 0) return cudaSuccess;
-  if (m > 128) return cudaErrorInvalidValue;
+// Q_v[:, col_v] = V_v, BQ_v[:, col_v] = BV_v (and their complex64 copies when
+// given) for every v with col_v >= 0.
+__global__ void k_gs_store(double2* __restrict__ Q, double2* __restrict__ BQ, float2* __restrict__ Q32,
+                           float2* __restrict__ BQ32, long long xs, const double2* __restrict__ V,
+                           const double2* __restrict__ BV, long long len, const int* __restrict__ col) {
+  const int v = blockIdx.y;
+  const int c = col[v];
+  if (c < 0) return;
+  const long long o = v * xs + (long long)c * len;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    const double2 a = V[v * len + i], b = BV[v * len + i];
+    Q[o + i] = a;
+    BQ[o + i] = b;
+    if (Q32) {
+      Q32[o + i] = make_float2(float(a.x), float(a.y));
+      BQ32[o + i] = make_float2(float(b.x), float(b.y));
+    }
+  }
+}
+
+cudaError_t gs_store(double2* Q, double2* BQ, float2* Q32, float2* BQ32, long long xs, const double2* V,
+                     const double2* BV, long long len, int nv, const int* col, cudaStream_t st) {
+  if (nv <= 0) return cudaSuccess;
+  int gx = grid_for(len);
+  if (gx > 1024) gx = 1024;
   FAME_LAUNCHED(1);
-  k_sub_combo_lo<<<grid_for(len), 256, 0, st>>>(r, X, len, ld, m, c);
+  k_gs_store<<<dim3(gx, nv), 256, 0, st>>>(Q, BQ, Q32, BQ32, xs, V, BV, len, col);
+  return cudaGetLastError();
+}
+
+cudaError_t gs_dots(const double2* X, long long xs, const double2* r, long long rs, long long len, int nv,
+                    const int2* span, int maxm, double2* coef, int cstride, double2* partial, int nblk,
+                    cudaStream_t st) {
+  if (nv <= 0 || maxm <= 0) return cudaSuccess;
+  FAME_LAUNCHED(1);
+  k_gs_dot_partial<<<dim3(nblk, nv, maxm), kRedThreads, 0, st>>>(X, xs, r, rs, len, span, maxm, partial);
+  FAME_LAUNCHED(1);
+  k_gs_dot_final<<<nv * maxm, kRedThreads, 0, st>>>(partial, nblk, maxm, span, coef, cstride);
+  return cudaGetLastError();
+}
+
+cudaError_t gs_combo(double2* r, long long rs, const double2* X, long long xs, long long len, int nv,
+                     const int2* span, const double2* coef, int cstride, cudaStream_t st) {
+  if (nv <= 0) return cudaSuccess;
+  int gx = grid_for(len);
+  if (gx > 1024) gx = 1024;
+  FAME_LAUNCHED(1);
+  k_gs_combo<double2><<<dim3(gx, nv), 256, 0, st>>>(r, rs, X, xs, len, span, coef, cstride);
+  return cudaGetLastError();
+}
+
+cudaError_t gs_combo_lo(double2* r, long long rs, const float2* X, long long xs, long long len, int nv,
+                        const int2* span, const double2* coef, int cstride, cudaStream_t st) {
+  if (nv <= 0) return cudaSuccess;
+  int gx = grid_for(len);
+  if (gx > 1024) gx = 1024;
+  FAME_LAUNCHED(1);
+  k_gs_combo<float2><<<dim3(gx, nv), 256, 0, st>>>(r, rs, X, xs, len, span, coef, cstride);
   return cudaGetLastError();
 }
 

@@ -22,7 +22,7 @@ enum WsId {
   WS_MIX_B32, WS_MIX_X32, WS_MIX_RES, WS_MIX_MASK, WS_MIX_BD, WS_PCG_Z,
   WS_LZ_Q, WS_LZ_BQ, WS_LZ_VEC, WS_LZ_TMP, WS_LZ_COEF, WS_LZ_INST, WS_LZ_MASK, WS_LZ_U, WS_LZ_SCAL, WS_LZ_DOT,
   WS_LZ_PART,
-  WS_LZ_Q32 = 190, WS_LZ_BQ32,
+  WS_LZ_Q32 = 190, WS_LZ_BQ32, WS_LZ_GSPART, WS_LZ_SPAN,
   WS_RF_X = 200, WS_RF_AX, WS_RF_BX, WS_RF_Y, WS_RF_BY, WS_RF_AY, WS_RF_R, WS_RF_Z, WS_RF_INST, WS_RF_G, WS_RF_C,
   WS_RF_PART
 };
@@ -697,26 +697,6 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     FAME_CK(scale_batched<double>(x, y, L, na, dsc, dmask, st), "lanczos scale");
     return FAME_OK;
   };
-  // r -= sum_i c_i X_i (and the same on BX when given), c on device
-  auto project_out = [&](int a, double2* r, double2* br, int col0, int m) -> int {
-    double2* Qa = Q + (size_t)a * p * L;
-    double2* BQa = BQ + (size_t)a * p * L;
-    double2* ca = coef + (size_t)a * 128;
-    FAME_CK(dot_batched<double>(BQa + (size_t)col0 * L, 0, L, m, r, 0, L, 1, ca, part, nblk1, nullptr, st),
-            "lanczos gs dot");
-    FAME_CK(sub_combo<double>(r, Qa + (size_t)col0 * L, L, L, m, ca, st), "lanczos gs");
-    if (br) FAME_CK(sub_combo<double>(br, BQa + (size_t)col0 * L, L, L, m, ca, st), "lanczos gs");
-    return FAME_OK;
-  };
-  auto sub_host = [&](int a, double2* r, double2* br, int col0, std::vector<double2> cs) -> int {
-    double2* Qa = Q + (size_t)a * p * L;
-    double2* BQa = BQ + (size_t)a * p * L;
-    double2* ca = coef + (size_t)a * 128 + 64;
-    FAME_CK(h2d_async(P, ca, cs.data(), sizeof(double2) * cs.size()), "lanczos");
-    FAME_CK(sub_combo<double>(r, Qa + (size_t)col0 * L, L, L, (int)cs.size(), ca, st), "lanczos");
-    if (br) FAME_CK(sub_combo<double>(br, BQa + (size_t)col0 * L, L, L, (int)cs.size(), ca, st), "lanczos");
-    return FAME_OK;
-  };
   const bool mixed = prec == FAME_C64;
   long long total_b = 0;
   // Mixed form: complex64 copies of Q and B*Q for the corrections of the full
@@ -739,17 +719,40 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     FAME_CK((convert<float, double>(BQ + o, BQ32 + o, L * m, st)), "lanczos lo copy");
     return FAME_OK;
   };
-  // reorthogonalisation against columns col0 .. col0+m-1: FP64 coefficients,
-  // corrections from the complex64 copies
-  auto project_out_lo = [&](int a, double2* r, double2* br, int col0, int m) -> int {
-    const double2* BQa = BQ + (size_t)a * p * L;
-    const float2* Q32a = Q32 + (size_t)a * p * L;
-    const float2* BQ32a = BQ32 + (size_t)a * p * L;
-    double2* ca = coef + (size_t)a * 128;
-    FAME_CK(dot_batched<double>(BQa + (size_t)col0 * L, 0, L, m, r, 0, L, 1, ca, part, nblk1, nullptr, st),
-            "lanczos gs dot");
-    FAME_CK(sub_combo_lo(r, Q32a + (size_t)col0 * L, L, L, m, ca, st), "lanczos gs");
-    if (br) FAME_CK(sub_combo_lo(br, BQ32a + (size_t)col0 * L, L, L, m, ca, st), "lanczos gs");
+  // Batched Gram-Schmidt: every instance of the batch in one launch per
+  // operation, instance a against its own columns span[a] = (col0, m)
+  // (m = 0: untouched).  Spans go to one of kSpanSlots device slots in turn
+  // (stream-ordered uploads, so consecutive operations may reuse a slot).
+  constexpr int kSpanSlots = 8;
+  int2* dspan = (int2*)workspace(P, WS_LZ_SPAN, sizeof(int2) * (size_t)na * kSpanSlots + sizeof(int) * na + 64, &e);
+  FAME_CK(e, "lanczos workspace");
+  int* dcol = (int*)(dspan + (size_t)na * kSpanSlots);
+  const int nblkg = dot_blocks(P, L, na);
+  double2* gspart = (double2*)workspace(P, WS_LZ_GSPART, sizeof(double2) * (size_t)na * 128 * nblkg + 64, &e);
+  FAME_CK(e, "lanczos workspace");
+  int span_slot = 0;
+  auto upload_span = [&](const std::vector<int2>& sp, int* maxm) -> const int2* {
+    int2* d = dspan + (size_t)na * (span_slot++ % kSpanSlots);
+    *maxm = 0;
+    for (const int2& q : sp) *maxm = std::max(*maxm, q.y);
+    if (h2d_async(P, d, sp.data(), sizeof(int2) * na) != cudaSuccess) return nullptr;
+    return d;
+  };
+  const long long qs = (long long)p * L;  // instance stride of Q, BQ and their copies
+  // r_a -= sum (B q_i)^H r_a q_i over span (and B r likewise), FP64 or with complex64 corrections
+  auto project_b = [&](const std::vector<int2>& sp, bool lo) -> int {
+    int maxm = 0;
+    const int2* d = upload_span(sp, &maxm);
+    if (!d) return cuda_fail(&P, cudaErrorUnknown, "lanczos span upload");
+    if (maxm == 0) return FAME_OK;
+    FAME_CK(gs_dots(BQ, qs, PR, L, L, na, d, maxm, coef, 128, gspart, nblkg, st), "lanczos gs dot");
+    if (lo) {
+      FAME_CK(gs_combo_lo(PR, L, Q32, qs, L, na, d, coef, 128, st), "lanczos gs");
+      if (mixed) FAME_CK(gs_combo_lo(BPR, L, BQ32, qs, L, na, d, coef, 128, st), "lanczos gs");
+    } else {
+      FAME_CK(gs_combo(PR, L, Q, qs, L, na, d, coef, 128, st), "lanczos gs");
+      if (mixed) FAME_CK(gs_combo(BPR, L, BQ, qs, L, na, d, coef, 128, st), "lanczos gs");
+    }
     return FAME_OK;
   };
 
@@ -805,13 +808,12 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     }
     if (!any) break;
     FAME_CK(upload_mask(), "lanczos mask");
-    // Q(:, j) = v ; BQ(:, j) = B v
-    for (int a = 0; a < na; ++a) {
-      if (S[a].done) continue;
-      const int j = S[a].j - 1;
-      FAME_CK(cudaMemcpyAsync(Q + ((size_t)a * p + j) * L, V + (size_t)a * L, cb, cudaMemcpyDeviceToDevice, st), "lz");
-      FAME_CK(cudaMemcpyAsync(BQ + ((size_t)a * p + j) * L, BV + (size_t)a * L, cb, cudaMemcpyDeviceToDevice, st), "lz");
-      if (int rc2 = copy_lo(a, j, 1)) return rc2;
+    // Q(:, j) = v ; BQ(:, j) = B v (and the complex64 copies), all instances in one launch
+    {
+      std::vector<int> colv(na);
+      for (int a = 0; a < na; ++a) colv[a] = S[a].done ? -1 : S[a].j - 1;
+      FAME_CK(h2d_async(P, dcol, colv.data(), sizeof(int) * na), "lz");
+      FAME_CK(gs_store(Q, BQ, Q32, BQ32, qs, V, BV, L, na, dcol, st), "lz");
     }
     // r = fncA(q); alpha = real(r'*q)   (Lanczos.m:50-51)
     FAME_CK(launch_fncA<double>(P, V, AQ, na, ctx, st), "lanczos fncA");
@@ -851,51 +853,69 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
     // (||c||^2 > ||r||_B^2 / 2, the DGKS test).  The mixed form carries B r,
     // which gives ||r||_B; the FP64 form always takes the second pass.
     std::vector<int> second(na, 0);
-    for (int a = 0; a < na; ++a) {
-      if (S[a].done) continue;
-      LzInst& I = S[a];
-      const int j = I.j - 1;
-      const double alpha = al[a].x;
-      I.Alpha.push_back(alpha);
-      double2* r = PR + (size_t)a * L;
-      double2* br = mixed ? BPR + (size_t)a * L : nullptr;
-      if (I.j == 1) {
-        if ((rc = sub_host(a, r, br, j, {make_double2(alpha, 0.0)}))) return rc;
-      } else if (I.justRestarted) {
-        if ((rc = project_out(a, r, br, 0, I.j))) return rc;
+    {
+      // r -= alpha q_j (- beta q_{j-1}) (Lanczos.m:55,62), coefficients from the host
+      std::vector<int2> sp(na, make_int2(0, 0)), sp63(na, make_int2(0, 0)), sp66(na, make_int2(0, 0)),
+          spfull(na, make_int2(0, 0));
+      std::vector<double2> hcf((size_t)na * 128, make_double2(0.0, 0.0));
+      for (int a = 0; a < na; ++a) {
+        if (S[a].done) continue;
+        LzInst& I = S[a];
+        const int j = I.j - 1;
+        const double alpha = al[a].x;
+        I.Alpha.push_back(alpha);
+        if (I.j == 1) {
+          sp[a] = make_int2(j, 1);
+          hcf[(size_t)a * 128] = make_double2(alpha, 0.0);
+        } else if (I.justRestarted) {
+          sp63[a] = make_int2(0, I.j);  // Lanczos.m:58-59, full pass with O(1) coefficients: FP64
+        } else {
+          sp[a] = make_int2(j - 1, 2);
+          hcf[(size_t)a * 128] = make_double2(I.beta, 0.0);
+          hcf[(size_t)a * 128 + 1] = make_double2(alpha, 0.0);
+          sp63[a] = make_int2(j - 1, 1);  // :63
+        }
+        sp66[a] = make_int2(j, 1);       // :66
+        spfull[a] = make_int2(0, I.j);   // :69
+        second[a] = 1;
         I.justRestarted = false;
-      } else {
-        if ((rc = sub_host(a, r, br, j - 1, {make_double2(I.beta, 0.0), make_double2(alpha, 0.0)}))) return rc;
-        if ((rc = project_out(a, r, br, j - 1, 1))) return rc;  // :63
+        I.steps++;
+        n_first++;
       }
-      if ((rc = project_out(a, r, br, j, 1))) return rc;  // :66
-      if (mixed)  // ||r||_B^2 before the full pass, next to the pass's coefficients
-        FAME_CK(dot_batched<double>(r, 0, L, 1, br, 0, L, 1, coef + (size_t)a * 128 + 127, part, nblk1, nullptr, st),
-                "lanczos norm");
-      if ((rc = mixed ? project_out_lo(a, r, br, 0, I.j) : project_out(a, r, br, 0, I.j))) return rc;  // :69
-      second[a] = 1;
-      n_first++;
-      I.steps++;
+      int maxm = 0;
+      const int2* d = upload_span(sp, &maxm);
+      if (!d) return cuda_fail(&P, cudaErrorUnknown, "lanczos span upload");
+      FAME_CK(h2d_async(P, coef, hcf.data(), sizeof(double2) * hcf.size()), "lanczos gs");
+      if (maxm > 0) {
+        FAME_CK(gs_combo(PR, L, Q, qs, L, na, d, coef, 128, st), "lanczos gs");
+        if (mixed) FAME_CK(gs_combo(BPR, L, BQ, qs, L, na, d, coef, 128, st), "lanczos gs");
+      }
+      if ((rc = project_b(sp63, false))) return rc;
+      if ((rc = project_b(sp66, false))) return rc;
+      if (mixed)  // ||r||_B^2 before the full pass (DGKS test below)
+        FAME_CK(dot_batched<double>(PR, L, 0, 1, BPR, L, L, na, ddot + na, part, nblkb, dmask, st), "lanczos norm");
+      if ((rc = project_b(spfull, mixed))) return rc;  // :69, first pass
     }
     if (mixed) {
-      std::vector<double2> hc((size_t)na * 128);
+      std::vector<double2> hc((size_t)na * 128), rbn(na);
       FAME_CK(cudaMemcpyAsync(hc.data(), coef, sizeof(double2) * hc.size(), cudaMemcpyDeviceToHost, st), "lanczos gs");
+      FAME_CK(cudaMemcpyAsync(rbn.data(), ddot + na, sizeof(double2) * na, cudaMemcpyDeviceToHost, st), "lanczos gs");
       FAME_CK(cudaStreamSynchronize(st), "lanczos gs");
       for (int a = 0; a < na; ++a) {
         if (!second[a]) continue;
         double c2 = 0.0;
         for (int i = 0; i < S[a].j; ++i) c2 += hc[(size_t)a * 128 + i].x * hc[(size_t)a * 128 + i].x +
                                                hc[(size_t)a * 128 + i].y * hc[(size_t)a * 128 + i].y;
-        const double r2 = hc[(size_t)a * 128 + 127].x;
-        second[a] = !(c2 <= 0.5 * r2);
+        second[a] = !(c2 <= 0.5 * rbn[a].x);
         n_second += second[a];
       }
     }
-    for (int a = 0; a < na; ++a)
-      if (second[a] && !S[a].done)
-        if ((rc = mixed ? project_out_lo(a, PR + (size_t)a * L, BPR + (size_t)a * L, 0, S[a].j)
-                        : project_out(a, PR + (size_t)a * L, nullptr, 0, S[a].j)))
-          return rc;
+    {
+      std::vector<int2> sp2(na, make_int2(0, 0));
+      for (int a = 0; a < na; ++a)
+        if (second[a] && !S[a].done) sp2[a] = make_int2(0, S[a].j);
+      if ((rc = project_b(sp2, mixed))) return rc;  // :69, second pass
+    }
     prof.mark(2);
     // rr = fncB(r); beta = sqrt(r'*rr); v = r/beta  (Lanczos.m:72-74)
     if (!mixed) {

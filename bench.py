@@ -25,6 +25,7 @@ import os
 import statistics
 import subprocess
 import sys
+import threading
 import time
 
 import numpy as np
@@ -204,8 +205,11 @@ def run_fame(args):
     lib = fame.load()
     path, batches, bidx_path = path_batches(args.batch)
     nb = len(batches)
+    C = max(1, args.concurrent)
+    # step s solves batches bidx(s*C) .. bidx(s*C + C - 1), C of them at once
     bidx = lambda s: batch_index(s, rank, world, nb)
-    needed = sorted({bidx(s) for s in range(args.warmup + args.steps)})
+    step_batches = lambda s: [bidx(s * C + c) for c in range(C)]
+    needed = sorted({b for s in range(args.warmup + args.steps) for b in step_batches(s)})
     plans = {b: fame.woodpile_plan(N_GRID, batches[b]) for b in needed}
     # fncB launch parameters timed once on one plan (fame_autotune) and
     # installed on every plan of the run (fame_set_tune)
@@ -225,8 +229,43 @@ def run_fame(args):
     def solve(plan):
         return plan.band_solve(BANDS, tol=args.lanczos_tol, prec="c64", inner_tol=INNER_TOL_MIXED, p=args.lanczos_p)
 
+    # C batches at once: each on its own CUDA stream, driven by its own host
+    # thread (distinct plans may run concurrently; one plan may not), so the
+    # kernels of one batch fill the GPU while the other waits on the host
+    # (convergence checks, Gram-Schmidt tests, restarts) or runs its last
+    # k-points.  Each stream starts after `start` and the caller's stream
+    # waits for all of them.
+    side = [torch.cuda.Stream() for _ in range(C)]
+
+    def solve_step(batch_ids, start=None, make_plan=None):
+        outs, errs = [None] * len(batch_ids), []
+
+        def work(c, b):
+            try:
+                with torch.cuda.stream(side[c]):
+                    if start is not None:
+                        side[c].wait_event(start)
+                    outs[c] = make_plan(b) if make_plan else solve(plans[b])
+            except Exception as ex:  # noqa: BLE001 - re-raised below
+                errs.append(ex)
+
+        if len(batch_ids) == 1:
+            work(0, batch_ids[0])
+        else:
+            th = [threading.Thread(target=work, args=(c, b)) for c, b in enumerate(batch_ids)]
+            for t_ in th:
+                t_.start()
+            for t_ in th:
+                t_.join()
+        cur = torch.cuda.current_stream()
+        for sd in side[:len(batch_ids)]:
+            cur.wait_stream(sd)
+        if errs:
+            raise errs[0]
+        return outs
+
     for s in range(args.warmup):
-        solve(plans[bidx(s)])
+        solve_step(step_batches(s))
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -237,9 +276,11 @@ def run_fame(args):
     launches0 = lib.fame_kernel_launches()
     clocks.start()
     e0.record(stream)
-    results = []
+    results, result_batches = [], []
     for s in range(args.steps):
-        results.append(solve(plans[bidx(args.warmup + s)]))
+        ids = step_batches(args.warmup + s)
+        results += solve_step(ids, start=e0)
+        result_batches += ids
     e1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -248,13 +289,13 @@ def run_fame(args):
         dist.barrier()
     t = e0.elapsed_time(e1) / 1000.0
     tmax = max_over_ranks(t, device="cuda")
-    value = whole_job_rate(args.batch, args.steps, world, tmax)
+    value = whole_job_rate(args.batch * C, args.steps, world, tmax)
     res_max = max(float(np.max(r["res"])) for r in results)
     worst = None
     for s, r in enumerate(results):
         i, j = np.unravel_index(int(np.argmax(r["res"])), r["res"].shape)
         if worst is None or r["res"][i, j] > worst["res"]:
-            worst = {"path_index": int(bidx_path[bidx(args.warmup + s)][i]), "band": int(j),
+            worst = {"path_index": int(bidx_path[result_batches[s]][i]), "band": int(j),
                      "res": float(r["res"][i, j]), "omega": float(r["omega"][i, j])}
     status = [int(r["status"]) for r in results]
     rb = [r["res_before"] for r in results if r.get("res_before") is not None]
@@ -281,17 +322,22 @@ def run_fame(args):
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for s in range(e2e_steps):
-        kv = batches[bidx(s)]
+    def e2e_batch(b):
+        kv = batches[b]
         th = np.stack([fame.bloch_angles(k, A) for k in kv])
         with fame.Plan(N_GRID, th, phase_host, tens) as pl:
             set_tune(pl)
             r = pl.band_solve(BANDS, tol=args.lanczos_tol, prec="c64", inner_tol=INNER_TOL_MIXED, p=args.lanczos_p)
-        h2d += phase_host.nbytes + th.nbytes + tens.nbytes * len(kv)
-        d2h += r["ew"].nbytes + r["res"].nbytes + r["stats"].nbytes
+        return r, phase_host.nbytes + th.nbytes + tens.nbytes * len(kv), \
+            r["ew"].nbytes + r["res"].nbytes + r["stats"].nbytes
+
+    for s in range(e2e_steps):
+        for r, hb, db in solve_step(step_batches(s), make_plan=e2e_batch):
+            h2d += hb
+            d2h += db
     torch.cuda.synchronize()
     te = max_over_ranks(time.perf_counter() - t0, device="cuda")
-    e2e_value = whole_job_rate(args.batch, e2e_steps, world, te) if e2e_steps else None
+    e2e_value = whole_job_rate(args.batch * C, e2e_steps, world, te) if e2e_steps else None
 
     out = None
     if rank == 0:
@@ -331,7 +377,7 @@ def run_fame(args):
             kv = batches[fb][:args.fp64_kpoints]
             ew_mixed = None
             for s, r in enumerate(results):
-                if bidx(args.warmup + s) == fb:
+                if result_batches[s] == fb:
                     ew_mixed = r["ew"][:args.fp64_kpoints]
             if ew_mixed is None:
                 pm = fame.woodpile_plan(N_GRID, kv)
@@ -378,7 +424,7 @@ def run_fame(args):
             "warmup": args.warmup, "ms_per_step": round(tmax / args.steps * 1e3, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64/f64", "data": "synthetic (woodpile geometry, "
             "band path generated in-run)",
-            "config": dict(workload_config(args.batch),
+            "config": dict(workload_config(args.batch * C), batches_at_once=C, kpoints_per_batch=args.batch,
                            lanczos_p=args.lanczos_p, lanczos_tol_mixed=args.lanczos_tol,
                            batching="consecutive path points, the two Gamma points in one batch",
                            fncb_tune={"chunk": int(tune["chunk"]), "stencil_tpb": int(tune["stencil_tpb"])},
@@ -562,6 +608,8 @@ def main():
                     help="k-points per step (batched band solve); 10 = the 40-point path in four steps, whose "
                          "fncB runs as two sub-batches of 5 vectors (fills the last wave of plane-kernel CTAs)")
     ap.add_argument("--impl", choices=["fame", "reference"], default="fame")
+    ap.add_argument("--concurrent", type=int, default=1,
+                    help="batches solved at once per step, each on its own stream and host thread")
     ap.add_argument("--lanczos-tol", type=float, default=LANCZOS_TOL_MIXED,
                     help="Lanczos tolerance of the mixed form (the FP64 form keeps the reference's 1e-10)")
     ap.add_argument("--lanczos-p", type=int, default=LANCZOS_P_MIXED,
