@@ -6,8 +6,12 @@
 //                intermediates in L2, and some widths fill the last wave of
 //                CTAs better than others;
 //   stencil_tpb  the material stencil's form: 0 the single-pass k_sweep,
-//                128/256/512 threads per block of the two-kernel form.
-// No counterpart in the reference.
+//                128/256/512 threads per block of the two-kernel form;
+//   lanes        the plane kernels' split of each pencil: threads per pencil
+//                of the prime-factor split (every count compiled for the
+//                size, plane_lanes_alt) or 0, one thread per pencil.
+// chunk x stencil_tpb are timed with the size's default split, then every
+// split with the best of those.  No counterpart in the reference.
 #include <algorithm>
 #include <vector>
 
@@ -27,12 +31,16 @@ TuneEntry tune_for(const Plan& P, int prec, int nvec) {
   return d;
 }
 
+// Install t; cached graphs hold the kernels of the old parameters, so a
+// change drops them.
 static void put_tune(Plan& P, const TuneEntry& t) {
   for (TuneEntry& u : P.tune)
     if (u.prec == t.prec && u.nvec == t.nvec) {
+      if (u.chunk != t.chunk || u.stencil_tpb != t.stencil_tpb || u.lanes != t.lanes) free_graphs(P);
       u = t;
       return;
     }
+  free_graphs(P);
   P.tune.push_back(t);
 }
 
@@ -69,37 +77,57 @@ static int autotune_prec(Plan& P, int nvec, int reps, TuneEntry* best_out) {
   cudaEventCreate(&ev[1]);
   TuneEntry best;
   best.us = 1e300;
+  // median time of one fncB on the batch with t installed (microseconds)
+  auto time_one = [&](TuneEntry& t) -> cudaError_t {
+    put_tune(P, t);
+    cudaError_t e2 = launch_fncB<R>(P, x, y, nvec, ctx, w0, w1, st);  // warm-up
+    std::vector<float> ms;
+    for (int r = 0; r < reps && e2 == cudaSuccess; ++r) {
+      cudaEventRecord(ev[0], st);
+      e2 = launch_fncB<R>(P, x, y, nvec, ctx, w0, w1, st);
+      cudaEventRecord(ev[1], st);
+      if (e2 == cudaSuccess) e2 = cudaEventSynchronize(ev[1]);
+      float m = 0.f;
+      if (e2 == cudaSuccess) e2 = cudaEventElapsedTime(&m, ev[0], ev[1]);
+      ms.push_back(m);
+    }
+    if (e2 == cudaSuccess) {
+      std::sort(ms.begin(), ms.end());
+      t.us = 1e3 * double(ms[ms.size() / 2]);
+    }
+    return e2;
+  };
   for (int c : chunks)
     for (int tpb : {0, 128, 256, 512}) {
+      if (e != cudaSuccess) break;
       TuneEntry t;
       t.prec = prec;
       t.nvec = nvec;
       t.chunk = c == nvec ? 0 : c;
       t.stencil_tpb = tpb;
-      put_tune(P, t);
-      e = launch_fncB<R>(P, x, y, nvec, ctx, w0, w1, st);  // warm-up
-      std::vector<float> ms;
-      for (int r = 0; r < reps && e == cudaSuccess; ++r) {
-        cudaEventRecord(ev[0], st);
-        e = launch_fncB<R>(P, x, y, nvec, ctx, w0, w1, st);
-        cudaEventRecord(ev[1], st);
-        if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
-        float m = 0.f;
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&m, ev[0], ev[1]);
-        ms.push_back(m);
-      }
-      if (e != cudaSuccess) {
-        cudaEventDestroy(ev[0]);
-        cudaEventDestroy(ev[1]);
-        put_tune(P, saved);
-        return cuda_fail(&P, e, "autotune");
-      }
-      std::sort(ms.begin(), ms.end());
-      t.us = 1e3 * double(ms[ms.size() / 2]);
+      e = time_one(t);
+      if (e == cudaSuccess && t.us < best.us) best = t;
+    }
+  // the plane kernels' split, with the best chunk and stencil form
+  if (e == cudaSuccess && P.opt_plane_split && plane_split(P.n) > 0) {
+    std::vector<int> lanes = {0};
+    for (int i = 1; i < kPlaneLanesMax; ++i)
+      if (plane_lanes_alt(P.n, i) > 0) lanes.push_back(plane_lanes_alt(P.n, i));
+    const TuneEntry base = best;
+    for (int g : lanes) {
+      TuneEntry t = base;
+      t.lanes = g;
+      e = time_one(t);
+      if (e != cudaSuccess) break;
       if (t.us < best.us) best = t;
     }
+  }
   cudaEventDestroy(ev[0]);
   cudaEventDestroy(ev[1]);
+  if (e != cudaSuccess) {
+    put_tune(P, saved);
+    return cuda_fail(&P, e, "autotune");
+  }
   put_tune(P, best);
   *best_out = best;
   return FAME_OK;
@@ -130,12 +158,32 @@ int fame_set_tune(fame_plan_t h, int prec, int nvec, int chunk, int stencil_tpb)
   if (nvec < 1 || chunk < 0 || (stencil_tpb != 0 && stencil_tpb != 128 && stencil_tpb != 256 && stencil_tpb != 512) ||
       (prec != FAME_C64 && prec != FAME_C128))
     return fail(&P, FAME_ERR_BAD_ARG, "fame_set_tune: bad argument");
-  TuneEntry t;
-  t.prec = prec;
-  t.nvec = nvec;
+  TuneEntry t = tune_for(P, prec, nvec);  // keeps the width's split
   t.chunk = chunk >= nvec ? 0 : chunk;
   t.stencil_tpb = stencil_tpb;
   put_tune(P, t);
+  return FAME_OK;
+}
+
+int fame_set_tune_lanes(fame_plan_t h, int prec, int nvec, int lanes) {
+  if (!h) return FAME_ERR_BAD_ARG;
+  Plan& P = h->P;
+  if (nvec < 1 || lanes < -1 || lanes > 64 || (prec != FAME_C64 && prec != FAME_C128))
+    return fail(&P, FAME_ERR_BAD_ARG, "fame_set_tune_lanes: bad argument");
+  TuneEntry t = tune_for(P, prec, nvec);
+  t.lanes = lanes;
+  put_tune(P, t);
+  return FAME_OK;
+}
+
+int fame_get_tune(fame_plan_t h, int prec, int nvec, int* chunk, int* stencil_tpb, int* lanes) {
+  if (!h) return FAME_ERR_BAD_ARG;
+  Plan& P = h->P;
+  if (nvec < 1 || (prec != FAME_C64 && prec != FAME_C128)) return fail(&P, FAME_ERR_BAD_ARG, "fame_get_tune: bad argument");
+  const TuneEntry t = tune_for(P, prec, nvec);
+  if (chunk) *chunk = t.chunk;
+  if (stencil_tpb) *stencil_tpb = t.stencil_tpb;
+  if (lanes) *lanes = t.lanes;
   return FAME_OK;
 }
 

@@ -347,7 +347,7 @@ int fame_set_option(fame_plan_t h, int option, double value) {
       P.opt_precond = value != 0.0;
       return FAME_OK;
     case FAME_OPT_GRAPH:
-      P.opt_graph = value != 0.0;
+      P.opt_graph = value <= 0.0 ? 0 : value < 1.5 ? 1 : 2;
       return FAME_OK;
     case FAME_OPT_SIRA_NEAREST:
       P.opt_sira_nearest = value != 0.0;
@@ -358,6 +358,9 @@ int fame_set_option(fame_plan_t h, int option, double value) {
       return FAME_OK;
     case FAME_OPT_REFINE:
       P.opt_refine = value != 0.0;
+      return FAME_OK;
+    case FAME_OPT_C64_ROUND:
+      P.opt_c64_round = value != 0.0;
       return FAME_OK;
     case FAME_OPT_REFINE_TOL:
       if (!(value > 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: refine tol in (0, 1)");

@@ -37,6 +37,21 @@ inline VecCtx sub_ctx(const VecCtx& c, int v0) {
   return s;
 }
 
+// Threads per pencil of the split-pencil plane kernels of fncB for size n
+// (0: none compiled, one thread per pencil).
+FAME_HD constexpr int plane_split(int n) {
+  return n == 60 ? 3 : n == 48 ? 3 : n == 40 ? 5 : n == 36 ? 4 : n == 30 ? 3 : n == 24 ? 3 : n == 20 ? 4
+       : n == 12 ? 3 : 0;
+}
+
+// Lane counts compiled for size n (i = 0 the default, 0 past the last): the
+// autotuner's choices of the split.  n = 60 also has 60 = 4 * 15 and 5 * 12
+// (720 / 900 threads per CTA, 15 / 12 values per thread).
+FAME_HD constexpr int plane_lanes_alt(int n, int i) {
+  return i == 0 ? plane_split(n) : n == 60 ? (i == 1 ? 4 : i == 2 ? 5 : 0) : 0;
+}
+constexpr int kPlaneLanesMax = 3;
+
 // Launch parameters of the fncB sequence picked by fame_autotune for one
 // (precision, batch width): vectors per launch sequence and the material
 // stencil's form (single pass, or threads per block of the two-kernel form).
@@ -44,6 +59,7 @@ struct TuneEntry {
   int prec = 0, nvec = 0;
   int chunk = 0;         // 0: whole batch
   int stencil_tpb = 0;   // 0: single-pass k_sweep; 128/256/512: two-kernel form
+  int lanes = -1;        // threads per pencil of the plane kernels: -1 the size's default, 0 one
   double us = 0.0;       // measured time of one fncB on the batch
 };
 
@@ -81,7 +97,8 @@ struct Plan {
   // options (fame_set_option)
   int opt_precond = 1;                // CG on B preconditioned by the averaged-medium B0^{-1}
   double opt_tol32 = 1e-6;            // complex64 CG tolerance of the first refinement round
-  int opt_graph = 1;                  // replay CG iterations from captured CUDA graphs
+  int opt_c64_round = 1;              // mixed B^{-1}: second round's B x update in complex64 (0: FP64 apply)
+  int opt_graph = 2;                  // CG from CUDA graphs: 1 blocks of iterations, 2 the whole loop
   double opt_itol_floor = 1e-13;      // mixed form: floor of the spread-scaled inner tolerance
   int opt_plane_split = 1;            // fncB plane kernels with several threads per pencil where compiled
   int opt_pi_table = 1;               // complex128 fncB reads Pi from the plan's table (else evaluates it)
@@ -196,10 +213,25 @@ template <class R> cudaError_t build_precond(Plan& P, cudaStream_t st);
 template <class R>
 cudaError_t precond_apply(const Plan& P, const cx<R>* r, cx<R>* z, int nvec, const VecCtx& ctx, double2* partial,
                           int nblk, cudaStream_t st);
+// The CG step length computed inside the update instead of by a separate
+// scalar kernel: every CTA of vector v reduces v's `nblk` partial sums of
+// p^H q in one fixed order, so all of them use the same alpha = rho / p^H q;
+// CTA 0 records alpha and the dot, and on breakdown (p^H q <= 0 or not
+// finite) clears active[v] and negates the iteration count (alpha 0).
+struct CgAlpha {
+  const double2* pq = nullptr;  // [nvec][nblk] partial sums, or null: alpha given
+  int nblk = 0;
+  const double* rho = nullptr;
+  double* alpha = nullptr;
+  double2* dot = nullptr;
+  int* active = nullptr;
+  int* iters = nullptr;
+};
 // x += a p ; r -= a q ; z = M r ; partial (Re r'z, |r|^2)
 template <class R>
 cudaError_t pcg_update(const Plan& P, cx<R>* x, cx<R>* r, cx<R>* z, const cx<R>* p, const cx<R>* q, int nvec,
-                       const VecCtx& ctx, const double* alpha, double2* partial, int nblk, cudaStream_t st);
+                       const VecCtx& ctx, const double* alpha, double2* partial, int nblk, cudaStream_t st,
+                       const CgAlpha& ca = CgAlpha());
 
 bool n_supported(int n);
 

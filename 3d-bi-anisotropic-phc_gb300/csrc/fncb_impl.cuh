@@ -343,9 +343,11 @@ k_plane_fwd(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, V
 // (N = 60: G = 3, 540 threads, 34 warps per SM against 12 for one thread per
 // 60-point pencil).
 // ---------------------------------------------------------------------------
-FAME_HD constexpr int plane_split(int n) {
-  return n == 60 ? 3 : n == 48 ? 3 : n == 40 ? 5 : n == 36 ? 4 : n == 30 ? 3 : n == 24 ? 3 : n == 20 ? 4
-       : n == 12 ? 3 : 0;
+
+// CTAs per SM the split kernels are compiled for: two for the default lane
+// count in complex64, one otherwise (the register allocation then decides).
+template <class R, int N, int G> constexpr int plane_min_blocks() {
+  return sizeof(R) == 4 && G == plane_split(N) ? 2 : 1;
 }
 
 template <int N, int G> struct Split {
@@ -399,11 +401,10 @@ template <int G, class F> __device__ __forceinline__ void with_g(int g, F&& f) {
   });
 }
 
-template <class R, int N, bool PREP_UNUSED = true>
-__global__ void __launch_bounds__(Split<N, plane_split(N)>::TB, sizeof(R) == 4 ? 2 : 1)
+template <class R, int N, int G>
+__global__ void __launch_bounds__(Split<N, G>::TB, plane_min_blocks<R, N, G>())
 k_plane_inv2(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d, VecCtx ctx,
              long long in_stride, long long in_side_stride, long long out_stride, int side0, DirUpd<R> upd) {
-  constexpr int G = plane_split(N);
   using SP = Split<N, G>;
   constexpr int M = SP::M, T = SP::T, LD = N + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -503,11 +504,10 @@ k_plane_inv2(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d
   }
 }
 
-template <class R, int N, bool POST_UNUSED = true>
-__global__ void __launch_bounds__(Split<N, plane_split(N)>::TB, sizeof(R) == 4 ? 2 : 1)
+template <class R, int N, int G>
+__global__ void __launch_bounds__(Split<N, G>::TB, plane_min_blocks<R, N, G>())
 k_plane_fwd2(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, VecCtx ctx,
              long long w_stride, long long out_stride, long long out_side_stride, int side0) {
-  constexpr int G = plane_split(N);
   using SP = Split<N, G>;
   constexpr int M = SP::M, T = SP::T, LD = N + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -631,20 +631,46 @@ inline dim3 grid_pts(long long Nq, int nvec, int tpb) {
   return dim3((unsigned)((Nq + tpb - 1) / tpb), (unsigned)nvec, 1);
 }
 
+// Lanes per pencil of the split plane kernels for a tuned value (< 0: the
+// default of size N; 0: one thread per pencil) under the plan's option;
+// a count not compiled for N falls back to the default.
+template <int N> inline int plane_lanes(const Plan& P, int tuned) {
+  if (!P.opt_plane_split || plane_split(N) == 0 || tuned == 0) return 0;
+  for (int i = 0; i < kPlaneLanesMax; ++i)
+    if (tuned > 0 && plane_lanes_alt(N, i) == tuned) return tuned;
+  return plane_split(N);
+}
+
+// f(integral_constant<G>) for the compiled lane count G == lanes of size N.
+template <int N, class F> inline void with_lanes(int lanes, F&& f) {
+  static_for<0, kPlaneLanesMax>([&](auto ic) {
+    constexpr int G = plane_lanes_alt(N, decltype(ic)::value);
+    if constexpr (G > 0)
+      if (lanes == G) f(std::integral_constant<int, G>{});
+  });
+}
+
 template <class R, int N, bool PREP, bool WITH_S>
 cudaError_t plane_inv(const Plan& P, const PlanData<R>& d, const cx<R>* x, cx<R>* out, int nvec,
                       int nside, int side0, long long in_stride, long long in_side_stride,
-                      long long out_stride, const VecCtx& ctx, cudaStream_t st, DirUpd<R> upd = DirUpd<R>()) {
+                      long long out_stride, const VecCtx& ctx, cudaStream_t st, DirUpd<R> upd = DirUpd<R>(),
+                      int tuned_lanes = -1) {
   const size_t sm = sizeof(cx<R>) * 3 * N * (N + 1);
   if constexpr (PREP && !WITH_S && plane_split(N) > 0) {
-    if (P.opt_plane_split) {
-      auto kfn = k_plane_inv2<R, N>;
-      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      if (e != cudaSuccess) return e;
-      FAME_LAUNCHED(1);
-      kfn<<<dim3(N, nside, nvec), Split<N, plane_split(N)>::TB, sm, st>>>(x, out, d, ctx, in_stride, in_side_stride,
-                                                                           out_stride, side0, upd);
-      return cudaGetLastError();
+    const int lanes = plane_lanes<N>(P, tuned_lanes);
+    if (lanes > 0) {
+      cudaError_t e = cudaErrorInvalidValue;
+      with_lanes<N>(lanes, [&](auto gc) {
+        constexpr int G = decltype(gc)::value;
+        auto kfn = k_plane_inv2<R, N, G>;
+        e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return;
+        FAME_LAUNCHED(1);
+        kfn<<<dim3(N, nside, nvec), Split<N, G>::TB, sm, st>>>(x, out, d, ctx, in_stride, in_side_stride,
+                                                               out_stride, side0, upd);
+        e = cudaGetLastError();
+      });
+      return e;
     }
   }
   const int threads = ((3 * N + 31) / 32) * 32;
@@ -660,17 +686,23 @@ cudaError_t plane_inv(const Plan& P, const PlanData<R>& d, const cx<R>* x, cx<R>
 template <class R, int N, bool POST, bool WITH_S>
 cudaError_t plane_fwd(const Plan& P, const PlanData<R>& d, const cx<R>* w, cx<R>* y, int nvec, int nside,
                       int side0, long long w_stride, long long out_stride, long long out_side_stride,
-                      const VecCtx& ctx, cudaStream_t st) {
+                      const VecCtx& ctx, cudaStream_t st, int tuned_lanes = -1) {
   const size_t sm = sizeof(cx<R>) * 3 * N * (N + 1);
   if constexpr (POST && !WITH_S && plane_split(N) > 0) {
-    if (P.opt_plane_split) {
-      auto kfn = k_plane_fwd2<R, N>;
-      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      if (e != cudaSuccess) return e;
-      FAME_LAUNCHED(1);
-      kfn<<<dim3(N, nside, nvec), Split<N, plane_split(N)>::TB, sm, st>>>(w, y, d, ctx, w_stride, out_stride,
-                                                                           out_side_stride, side0);
-      return cudaGetLastError();
+    const int lanes = plane_lanes<N>(P, tuned_lanes);
+    if (lanes > 0) {
+      cudaError_t e = cudaErrorInvalidValue;
+      with_lanes<N>(lanes, [&](auto gc) {
+        constexpr int G = decltype(gc)::value;
+        auto kfn = k_plane_fwd2<R, N, G>;
+        e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return;
+        FAME_LAUNCHED(1);
+        kfn<<<dim3(N, nside, nvec), Split<N, G>::TB, sm, st>>>(w, y, d, ctx, w_stride, out_stride,
+                                                               out_side_stride, side0);
+        e = cudaGetLastError();
+      });
+      return e;
     }
   }
   const int threads = ((3 * N + 31) / 32) * 32;
@@ -724,7 +756,7 @@ cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecC
       upd.z = pupd_z + (size_t)v0 * 4 * Nq;
       upd.beta = pupd_beta + v0;
     }
-    e = plane_inv<R, N, true, false>(P, d, xs, w0, nv, 2, 0, 4 * Nq, 2 * Nq, 6 * Nq, c, st, upd);
+    e = plane_inv<R, N, true, false>(P, d, xs, w0, nv, 2, 0, 4 * Nq, 2 * Nq, 6 * Nq, c, st, upd, tn.lanes);
     if (e != cudaSuccess) return e;
     e = col<R, N, +1, 0>(d, w0, 6, nv, 6 * Nq, c, st);
     if (e != cudaSuccess) return e;
@@ -739,7 +771,7 @@ cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecC
     if (e != cudaSuccess) return e;
     e = col<R, N, -1, 0>(d, wm, 6, nv, 6 * Nq, c, st);
     if (e != cudaSuccess) return e;
-    e = plane_fwd<R, N, true, false>(P, d, wm, ys, nv, 2, 0, 6 * Nq, 4 * Nq, 2 * Nq, c, st);
+    e = plane_fwd<R, N, true, false>(P, d, wm, ys, nv, 2, 0, 6 * Nq, 4 * Nq, 2 * Nq, c, st, tn.lanes);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

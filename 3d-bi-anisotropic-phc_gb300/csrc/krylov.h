@@ -30,6 +30,10 @@ cudaError_t cg_scalars(int stage, int nvec, const double2* dot, double* rho, dou
                        const double* tol2b2, int* active, int* iters, double* res2, cudaStream_t st);
 // cg_scalars on the sums of nblk partials per vector (partial[v * nblk + i]),
 // the sums also stored in dot[v]; one launch.
+// Condition kernel of a graph-resident loop (graph_replay_while): *passes
+// += 1, and the loop goes on while any active[v] and *passes < max_passes.
+cudaError_t while_active(const int* active, int nvec, int* passes, int max_passes, cudaGraphConditionalHandle h,
+                         cudaStream_t st);
 cudaError_t cg_scalars_red(int stage, int nvec, const double2* partial, int nblk, double2* dot, double* rho,
                            double* alpha, double* beta, const double* tol2b2, int* active, int* iters, double* res2,
                            cudaStream_t st);
@@ -80,9 +84,15 @@ cudaError_t sub_combo(cx<R>* r, const cx<R>* X, long long len, long long ld, int
                       cudaStream_t st);
 template <class D, class S>
 cudaError_t convert(const cx<S>* in, cx<D>* out, long long n, cudaStream_t st);
-cudaError_t refine_acc(double2* x, const float2* d, long long len, int nvec, const int* active, cudaStream_t st);
+// x += mult_v * d (mult null: 1)
+cudaError_t refine_acc(double2* x, const float2* d, long long len, int nvec, const int* active, cudaStream_t st,
+                       const double* mult = nullptr);
+// res = b - bx; res32 (may be null) its complex64 copy
 cudaError_t residual(const double2* b, const double2* bx, double2* res, float2* res32, long long len, int nvec,
                      const int* active, cudaStream_t st);
+// out = s_v * in, rounded to complex64
+cudaError_t to32_scaled(const double2* in, float2* out, long long len, int nvec, const double* s, const int* active,
+                        cudaStream_t st);
 template <class R>
 cudaError_t scale_batched(const cx<R>* x, cx<R>* y, long long len, int nvec, const double* s, const int* active,
                           cudaStream_t st);

@@ -425,17 +425,18 @@ __global__ void k_convert(const cx<S>* __restrict__ in, cx<D>* __restrict__ out,
     out[i] = mk<D>(D(in[i].x), D(in[i].y));
 }
 
-// x64 += d32 ; res = b - bx (both FP64) for active vectors
+// x64 += m_v * d32 (m null: m_v = 1); res = b - bx (both FP64) for active vectors
 __global__ void k_refine_acc(double2* __restrict__ x, const float2* __restrict__ d, long long len,
-                             const int* __restrict__ active) {
+                             const int* __restrict__ active, const double* __restrict__ mult) {
   const int vec = blockIdx.y;
   if (active && !active[vec]) return;
+  const double m = mult ? mult[vec] : 1.0;
   const long long o = vec * len;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
     double2 a = x[o + i];
     float2 b = d[o + i];
-    a.x += b.x;
-    a.y += b.y;
+    a.x += m * double(b.x);
+    a.y += m * double(b.y);
     x[o + i] = a;
   }
 }
@@ -447,7 +448,19 @@ __global__ void k_residual(const double2* __restrict__ b, const double2* __restr
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
     double2 r = make_double2(b[o + i].x - bx[o + i].x, b[o + i].y - bx[o + i].y);
     res[o + i] = r;
-    res32[o + i] = make_float2(float(r.x), float(r.y));
+    if (res32) res32[o + i] = make_float2(float(r.x), float(r.y));
+  }
+}
+// out32 = s_v * in (FP64 -> complex64) for active vectors
+__global__ void k_to32_scaled(const double2* __restrict__ in, float2* __restrict__ out, long long len,
+                              const double* __restrict__ s, const int* __restrict__ active) {
+  const int vec = blockIdx.y;
+  if (active && !active[vec]) return;
+  const double a = s[vec];
+  const long long o = vec * len;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    const double2 r = in[o + i];
+    out[o + i] = make_float2(float(a * r.x), float(a * r.y));
   }
 }
 // y = s_v * x per vector (real per-vector scalars), x and y may alias
@@ -602,6 +615,28 @@ cudaError_t gs_combo_lo(double2* r, long long rs, const float2* X, long long xs,
   return cudaGetLastError();
 }
 
+// The loop condition of a graph-resident iteration loop: one pass of the
+// body done (*passes + 1); continue while any vector is active and fewer
+// than max_passes passes have run.
+__global__ void k_while_active(const int* __restrict__ active, int nvec, int* __restrict__ passes, int max_passes,
+                               cudaGraphConditionalHandle h) {
+  int any = 0;
+  for (int v = threadIdx.x; v < nvec; v += blockDim.x) any |= active[v];
+  any = __any_sync(0xffffffffu, any);
+  if (threadIdx.x == 0) {
+    const int b = *passes + 1;
+    *passes = b;
+    cudaGraphSetConditional(h, (any && b < max_passes) ? 1u : 0u);
+  }
+}
+
+cudaError_t while_active(const int* active, int nvec, int* passes, int max_passes, cudaGraphConditionalHandle h,
+                         cudaStream_t st) {
+  FAME_LAUNCHED(1);
+  k_while_active<<<1, 32, 0, st>>>(active, nvec, passes, max_passes, h);
+  return cudaGetLastError();
+}
+
 cudaError_t cg_scalars_red(int stage, int nvec, const double2* partial, int nblk, double2* dot, double* rho,
                            double* alpha, double* beta, const double* tol2b2, int* active, int* iters, double* res2,
                            cudaStream_t st) {
@@ -681,11 +716,21 @@ cudaError_t convert(const cx<S>* in, cx<D>* out, long long n, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t refine_acc(double2* x, const float2* d, long long len, int nvec, const int* active, cudaStream_t st) {
+cudaError_t refine_acc(double2* x, const float2* d, long long len, int nvec, const int* active, cudaStream_t st,
+                       const double* mult) {
   int gx = grid_for(len);
   if (gx > 1024) gx = 1024;
   FAME_LAUNCHED(1);
-  k_refine_acc<<<dim3(gx, nvec), 256, 0, st>>>(x, d, len, active);
+  k_refine_acc<<<dim3(gx, nvec), 256, 0, st>>>(x, d, len, active, mult);
+  return cudaGetLastError();
+}
+
+cudaError_t to32_scaled(const double2* in, float2* out, long long len, int nvec, const double* s, const int* active,
+                        cudaStream_t st) {
+  int gx = grid_for(len);
+  if (gx > 1024) gx = 1024;
+  FAME_LAUNCHED(1);
+  k_to32_scaled<<<dim3(gx, nvec), 256, 0, st>>>(in, out, len, s, active);
   return cudaGetLastError();
 }
 

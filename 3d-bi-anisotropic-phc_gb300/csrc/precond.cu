@@ -203,7 +203,7 @@ template <class R>
 __global__ void __launch_bounds__(kThreads, sizeof(R) == 4 ? 2 : 1)
 k_pcg_update(cx<R>* __restrict__ x, cx<R>* __restrict__ r, cx<R>* __restrict__ z, const cx<R>* __restrict__ p,
              const cx<R>* __restrict__ q, const cx<R>* __restrict__ pc_all, VecCtx ctx, long long Nq,
-             const double* __restrict__ alpha, double2* __restrict__ partial) {
+             const double* __restrict__ alpha, double2* __restrict__ partial, CgAlpha ca) {
   const int vec = blockIdx.y;
   const int nblk = gridDim.x;
   double2* out = partial + (long long)vec * nblk + blockIdx.x;
@@ -211,7 +211,40 @@ k_pcg_update(cx<R>* __restrict__ x, cx<R>* __restrict__ r, cx<R>* __restrict__ z
     if (threadIdx.x == 0) *out = make_double2(0.0, 0.0);
     return;
   }
-  const R a = R(alpha[vec]);
+  R a;
+  if (ca.pq) {
+    __shared__ double s_alpha;
+    if (threadIdx.x < 32) {
+      double sx = 0.0, sy = 0.0;
+      for (int i = threadIdx.x; i < ca.nblk; i += 32) {
+        const double2 t = ca.pq[(long long)vec * ca.nblk + i];
+        sx += t.x;
+        sy += t.y;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_down_sync(0xffffffffu, sx, o);
+        sy += __shfl_down_sync(0xffffffffu, sy, o);
+      }
+      if (threadIdx.x == 0) {
+        const bool ok = sx > 0.0 && isfinite(sx);
+        const double av = ok ? ca.rho[vec] / sx : 0.0;
+        s_alpha = av;
+        if (blockIdx.x == 0) {
+          ca.alpha[vec] = av;
+          ca.dot[vec] = make_double2(sx, sy);
+          if (!ok) {  // breakdown: B must be HPD
+            ca.active[vec] = 0;
+            ca.iters[vec] = -(ca.iters[vec] + 1);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    a = R(s_alpha);
+  } else {
+    a = R(alpha[vec]);
+  }
   const cx<R>* pc = pc_all + (long long)vec_inst(ctx, vec) * kPcSlots * Nq;
   const long long o = vec * 4 * Nq;
   R srz = 0, srr = 0;
@@ -300,10 +333,11 @@ cudaError_t precond_apply(const Plan& P, const cx<R>* r, cx<R>* z, int nvec, con
 
 template <class R>
 cudaError_t pcg_update(const Plan& P, cx<R>* x, cx<R>* r, cx<R>* z, const cx<R>* p, const cx<R>* q, int nvec,
-                       const VecCtx& ctx, const double* alpha, double2* partial, int nblk, cudaStream_t st) {
+                       const VecCtx& ctx, const double* alpha, double2* partial, int nblk, cudaStream_t st,
+                       const CgAlpha& ca) {
   const PlanData<R>& d = detail::pdata<R>(P);
   FAME_LAUNCHED(1);
-  k_pcg_update<R><<<dim3(nblk, nvec), kThreads, 0, st>>>(x, r, z, p, q, d.pc, ctx, P.Nq, alpha, partial);
+  k_pcg_update<R><<<dim3(nblk, nvec), kThreads, 0, st>>>(x, r, z, p, q, d.pc, ctx, P.Nq, alpha, partial, ca);
   return cudaGetLastError();
 }
 
@@ -314,8 +348,8 @@ template cudaError_t precond_apply<float>(const Plan&, const float2*, float2*, i
 template cudaError_t precond_apply<double>(const Plan&, const double2*, double2*, int, const VecCtx&, double2*, int,
                                            cudaStream_t);
 template cudaError_t pcg_update<float>(const Plan&, float2*, float2*, float2*, const float2*, const float2*, int,
-                                       const VecCtx&, const double*, double2*, int, cudaStream_t);
+                                       const VecCtx&, const double*, double2*, int, cudaStream_t, const CgAlpha&);
 template cudaError_t pcg_update<double>(const Plan&, double2*, double2*, double2*, const double2*, const double2*, int,
-                                        const VecCtx&, const double*, double2*, int, cudaStream_t);
+                                        const VecCtx&, const double*, double2*, int, cudaStream_t, const CgAlpha&);
 
 }  // namespace fame

@@ -24,7 +24,7 @@ enum WsId {
   WS_LZ_PART,
   WS_LZ_Q32 = 190, WS_LZ_BQ32, WS_LZ_GSPART, WS_LZ_SPAN,
   WS_RF_X = 200, WS_RF_AX, WS_RF_BX, WS_RF_Y, WS_RF_BY, WS_RF_AY, WS_RF_R, WS_RF_Z, WS_RF_INST, WS_RF_G, WS_RF_C,
-  WS_RF_PART
+  WS_RF_PART, WS_PCG_PART2
 };
 
 #define FAME_CK(expr, where)                      \
@@ -60,6 +60,7 @@ static int dot_blocks(const Plan& P, long long len, int nvec) {
 struct CgScalars {
   double *rho, *alpha, *beta, *tol2b2, *res2;
   int *active, *iters;
+  int* passes;  // passes of the graph-resident iteration loop
   double2* dot;
 };
 
@@ -77,7 +78,7 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
   FAME_CK(e, "pcg workspace");
   cx<R>* q = (cx<R>*)workspace(P, WS_PCG_Q + (sizeof(R) == 4 ? 100 : 0), vb, &e);
   FAME_CK(e, "pcg workspace");
-  const size_t sb = (5 * sizeof(double) + 2 * sizeof(int) + sizeof(double2)) * nvec + 64;
+  const size_t sb = (5 * sizeof(double) + 2 * sizeof(int) + sizeof(double2)) * nvec + 4 * sizeof(int) + 64;
   char* s = (char*)workspace(P, WS_PCG_SCAL, sb, &e);
   FAME_CK(e, "pcg workspace");
   CgScalars S;
@@ -89,12 +90,15 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
   S.res2 = S.tol2b2 + nvec;
   S.active = (int*)(S.res2 + nvec);
   S.iters = S.active + nvec;
+  S.passes = S.iters + nvec;
   const int nblk = dot_blocks(P, L, nvec);
   // p^H B p from the stencil pass of fncB where its tuned form provides it
   const int nblk_pq = fncB_pq_partials<R>(P, nvec);
   const int nblkv0 = dot_blocks(P, P.Nq, nvec);
   const int npart = std::max(std::max(nblk, nblk_pq), nblkv0);
   double2* part = (double2*)workspace(P, WS_PCG_PART, sizeof(double2) * npart * nvec + 64, &e);
+  FAME_CK(e, "pcg workspace");
+  double2* part2 = (double2*)workspace(P, WS_PCG_PART2, sizeof(double2) * nblkv0 * nvec + 64, &e);
   FAME_CK(e, "pcg workspace");
   FAME_CK(ensure_work(P, nvec), "pcg fncB scratch");
   cx<R>* w0 = (cx<R>*)P.d_work;
@@ -164,29 +168,42 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
   //                                     beta = 0 before the first iteration;
   //                                     with the partials of p^H q when the
   //                                     stencil pass provides them)
-  //   alpha = rho / p^H q             (partials reduced in the same launch)
+  //   alpha = rho / p^H q             (preconditioned: reduced by the update
+  //                                     kernel itself; else one scalar launch)
   //   x += alpha p, r -= alpha q, z = M r, partials of (r^H z, |r|^2)
   //   beta, rho, convergence          (partials reduced in the same launch)
+  // Preconditioned, that is two glue launches per iteration.
+  CgAlpha ca;
+  if (pre) {
+    ca.pq = part;
+    ca.nblk = nblk_pq ? nblk_pq : nblk;
+    ca.rho = S.rho;
+    ca.alpha = S.alpha;
+    ca.dot = S.dot;
+    ca.active = S.active;
+    ca.iters = S.iters;
+  }
   auto iteration = [&](cudaStream_t cs) -> cudaError_t {
     cudaError_t e2 = launch_fncB<R>(P, p, q, nvec, ctx, w0, w1, cs, nblk_pq ? part : nullptr, pre ? z : r, S.beta);
     if (e2 == cudaSuccess && !nblk_pq) e2 = dot_partial<R>(p, q, L, L, nvec, part, nblk, S.active, cs);
-    if (e2 == cudaSuccess)
-      e2 = cg_scalars_red(0, nvec, part, nblk_pq ? nblk_pq : nblk, S.dot, S.rho, S.alpha, S.beta, S.tol2b2,
-                          S.active, S.iters, S.res2, cs);
     if (pre) {
-      if (e2 == cudaSuccess) e2 = pcg_update<R>(P, x, r, z, p, q, nvec, ctx, S.alpha, part, nblkv, cs);
-    } else if (e2 == cudaSuccess) {
-      e2 = cg_xr_partial<R>(x, r, p, q, L, L, nvec, S.alpha, S.active, part, nblk, cs);
+      // the update's own partial sums go to part2 (part still holds p^H q)
+      if (e2 == cudaSuccess) e2 = pcg_update<R>(P, x, r, z, p, q, nvec, ctx, S.alpha, part2, nblkv, cs, ca);
+    } else {
+      if (e2 == cudaSuccess)
+        e2 = cg_scalars_red(0, nvec, part, nblk, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active, S.iters,
+                            S.res2, cs);
+      if (e2 == cudaSuccess) e2 = cg_xr_partial<R>(x, r, p, q, L, L, nvec, S.alpha, S.active, part, nblk, cs);
     }
     if (e2 == cudaSuccess)
-      e2 = cg_scalars_red(1, nvec, part, pre ? nblkv : nblk, S.dot, S.rho, S.alpha, S.beta, S.tol2b2, S.active,
-                          S.iters, S.res2, cs);
+      e2 = cg_scalars_red(1, nvec, pre ? part2 : part, pre ? nblkv : nblk, S.dot, S.rho, S.alpha, S.beta, S.tol2b2,
+                          S.active, S.iters, S.res2, cs);
     return e2;
   };
   const int chk = 4;
   const std::vector<uintptr_t> gkey = {sizeof(R), (uintptr_t)nvec, (uintptr_t)pre, (uintptr_t)chk, (uintptr_t)P.n,
                                        (uintptr_t)p, (uintptr_t)q, (uintptr_t)x, (uintptr_t)r, (uintptr_t)z,
-                                       (uintptr_t)w0, (uintptr_t)w1, (uintptr_t)s, (uintptr_t)part,
+                                       (uintptr_t)w0, (uintptr_t)w1, (uintptr_t)s, (uintptr_t)part, (uintptr_t)part2,
                                        (uintptr_t)d_inst, (uintptr_t)nblk, (uintptr_t)nblkv,
                                        sizeof(R) == 4 ? (uintptr_t)P.d32.pc : (uintptr_t)P.d64.pc,
                                        (uintptr_t)tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).chunk,
@@ -195,7 +212,34 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
                                        (uintptr_t)P.opt_pi_table};
   bool use_graph = P.opt_graph != 0;
   bool any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
-  for (int it = 1; it <= maxit && any; it += chk) {
+  int it = 1;
+  if (P.opt_graph >= 2 && any && maxit >= chk) {
+    // the whole loop of chk-iteration blocks in one graph launch, the
+    // convergence test on the device after each block; the host waits once
+    std::vector<uintptr_t> wkey = gkey;
+    wkey.push_back((uintptr_t)0x5748494cu);  // distinct from the block graph
+    wkey.push_back((uintptr_t)(maxit / chk));
+    unsigned long long body_nodes = 0;
+    cudaError_t ge = graph_replay_while(P, wkey, [&](cudaStream_t cs) -> cudaError_t {
+      for (int i = 0; i < chk; ++i) {
+        cudaError_t e2 = iteration(cs);
+        if (e2 != cudaSuccess) return e2;
+      }
+      return cudaSuccess;
+    }, S.active, nvec, S.passes, maxit / chk, &body_nodes);
+    if (ge == cudaSuccess) {
+      int passes = 0;
+      FAME_CK(cudaMemcpyAsync(act.data(), S.active, sizeof(int) * nvec, cudaMemcpyDeviceToHost, st), "pcg check");
+      FAME_CK(cudaMemcpyAsync(&passes, S.passes, sizeof(int), cudaMemcpyDeviceToHost, st), "pcg check");
+      FAME_CK(cudaStreamSynchronize(st), "pcg check");
+      FAME_LAUNCHED(body_nodes * (unsigned long long)passes);
+      it = 1 + passes * chk;
+      any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
+    } else if (ge != cudaErrorNotSupported) {
+      FAME_CK(ge, "pcg graph loop");
+    }
+  }
+  for (; it <= maxit && any; it += chk) {
     const int nit = std::min(chk, maxit - it + 1);
     bool done = false;
     if (use_graph && nit == chk) {
@@ -255,11 +299,14 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
   double2* res = (double2*)workspace(P, WS_MIX_RES, sizeof(double2) * L * nvec, &e);
   FAME_CK(e, "mixed workspace");
   const int nblk = dot_blocks(P, L, nvec);
-  char* sc = (char*)workspace(P, WS_MIX_MASK, (sizeof(int) + sizeof(double2)) * nvec + sizeof(double2) * nblk * nvec + 64, &e);
+  char* sc = (char*)workspace(P, WS_MIX_MASK,
+                              (sizeof(int) + sizeof(double2)) * nvec + sizeof(double2) * nblk * nvec +
+                                  2 * sizeof(double) * nvec + 64, &e);
   FAME_CK(e, "mixed workspace");
   double2* dot = (double2*)sc;
   double2* part = dot + nvec;
-  int* dmask = (int*)(part + (size_t)nblk * nvec);
+  double* dscale = (double*)(part + (size_t)nblk * nvec);  // [nvec] 2^-e, [nvec] 2^e (e: exponent of ||res||)
+  int* dmask = (int*)(dscale + 2 * nvec);
   FAME_CK(ensure_work(P, nvec), "mixed scratch");
 
   std::vector<unsigned char> m(nvec, 1);
@@ -279,10 +326,30 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
     FAME_CK(cudaMemsetAsync(Bx + (size_t)v * L, 0, sizeof(double2) * L, st), "mixed init");
     if (!(bb[v].x > 0.0)) m[v] = 0;
   }
-  // res = b (FP64) and its complex64 copy
-  FAME_CK(residual(b, Bx, res, res32, L, nvec, dmask, st), "mixed residual");
+  // Each complex64 round solves B d = s res with s = 2^-e, e the binary
+  // exponent of ||res|| (a right-hand side of norm in [1, 2), so that no
+  // product in the complex64 CG underflows however small the residual has
+  // become; a power of two scales without rounding) and adds d / s to x.
+  std::vector<double> scl(2 * nvec, 1.0);
+  auto upload_scale = [&](const std::vector<double>& rr) -> cudaError_t {
+    for (int v = 0; v < nvec; ++v) {
+      const double nr = rr[v] > 0.0 && std::isfinite(rr[v]) ? std::sqrt(rr[v]) : 1.0;
+      const int ex = std::ilogb(nr);
+      scl[v] = std::ldexp(1.0, -ex);
+      scl[nvec + v] = std::ldexp(1.0, ex);
+    }
+    return h2d_async(P, dscale, scl.data(), sizeof(double) * 2 * nvec);
+  };
+  // res = b (FP64) and its scaled complex64 copy
+  FAME_CK(residual(b, Bx, res, nullptr, L, nvec, dmask, st), "mixed residual");
   for (int v = 0; v < nvec; ++v) mi[v] = m[v];
   FAME_CK(h2d_async(P, dmask, mi.data(), sizeof(int) * nvec), "mixed init");
+  {
+    std::vector<double> b2(nvec);
+    for (int v = 0; v < nvec; ++v) b2[v] = bb[v].x;
+    FAME_CK(upload_scale(b2), "mixed scale");
+    FAME_CK(to32_scaled(res, res32, L, nvec, dscale, dmask, st), "mixed scale");
+  }
   int rc = FAME_OK;
   std::vector<int> its(nvec);
   VecCtx ctx;
@@ -310,8 +377,8 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
         if (cg_iters) *cg_iters += std::abs(its[v]);
         if (cg_vec) cg_vec[v] += std::abs(its[v]);
       }
-    FAME_CK(refine_acc(x, d32, L, nvec, dmask, st), "mixed acc");
-    if (round != 1) {
+    FAME_CK(refine_acc(x, d32, L, nvec, dmask, st, dscale + nvec), "mixed acc");
+    if (round != 1 || !P.opt_c64_round) {
       // exact FP64 residual b - B x
       double2* w0 = (double2*)P.d_work;
       double2* w1 = w0 + (size_t)nvec * 6 * P.Nq;
@@ -321,14 +388,16 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
         if (b64_vec) b64_vec[v] += m[v];
       }
     } else {
-      // B x = (B x_prev) + B d with B d in complex64: d is already ~1e-6 of x,
-      // so its complex64 apply adds ~1e-13 relative error to B x.
+      // B x = (B x_prev) + B d with B d in complex64: d is already ~1e-6 of
+      // x, so the residual this estimates is good to ~1e-11 of b; a target
+      // below that takes a further round, whose FP64 apply makes B x exact
+      // again (B x is the B Q of the Lanczos basis).
       float2* w0 = (float2*)P.d_work;
       float2* w1 = w0 + (size_t)nvec * 6 * P.Nq;
       FAME_CK(launch_fncB<float>(P, d32, bd32, nvec, ctx, w0, w1, st), "mixed fncB32");
-      FAME_CK(refine_acc(Bx, bd32, L, nvec, dmask, st), "mixed acc");
+      FAME_CK(refine_acc(Bx, bd32, L, nvec, dmask, st, dscale + nvec), "mixed acc");
     }
-    FAME_CK(residual(b, Bx, res, res32, L, nvec, dmask, st), "mixed residual");
+    FAME_CK(residual(b, Bx, res, nullptr, L, nvec, dmask, st), "mixed residual");
     FAME_CK(dot_batched<double>(res, L, 0, 1, res, L, L, nvec, dot, part, nblk, dmask, st), "mixed dot");
     std::vector<double2> rr(nvec);
     FAME_CK(cudaMemcpyAsync(rr.data(), dot, sizeof(double2) * nvec, cudaMemcpyDeviceToHost, st), "mixed check");
@@ -341,6 +410,12 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
     }
     for (int v = 0; v < nvec; ++v) mi[v] = m[v];
     FAME_CK(h2d_async(P, dmask, mi.data(), sizeof(int) * nvec), "mixed mask");
+    if (round + 1 < max_rounds && std::any_of(m.begin(), m.end(), [](unsigned char a) { return a != 0; })) {
+      std::vector<double> r2(nvec);
+      for (int v = 0; v < nvec; ++v) r2[v] = rr[v].x;
+      FAME_CK(upload_scale(r2), "mixed scale");
+      FAME_CK(to32_scaled(res, res32, L, nvec, dscale, dmask, st), "mixed scale");
+    }
   }
   if (std::any_of(m.begin(), m.end(), [](unsigned char a) { return a != 0; })) rc = FAME_ERR_NOT_CONVERGED;
   return rc;
@@ -451,7 +526,12 @@ int ritz_refine(Plan& P, const std::vector<int>& insts, int k, double2* X, doubl
   long long cgi = 0, b64 = 0;
   rc = solve_B_mixed(P, Rv, W, BW, nv, dinst, tol, 8, P.opt_tol32, 4000, nullptr, &cgi, &b64, nullptr, cg_vec,
                      b64_vec);
-  if (rc == FAME_ERR_NAN || rc == FAME_ERR_BREAKDOWN) return rc;
+  if (rc == FAME_ERR_NAN || rc == FAME_ERR_BREAKDOWN) {
+    // no usable search direction: the pairs stay as the Lanczos run left them
+    if (res_after) std::copy(rb.begin(), rb.end(), res_after);
+    P.last_error.clear();
+    return FAME_OK;
+  }
   // W to unit B-norm (its norm is that of the residuals, ~1e-10, and would
   // otherwise vanish below the cut-off of the orthogonalisation)
   {

@@ -34,6 +34,7 @@ FAME_OPT_SIRA_NEAREST = 5
 FAME_OPT_REFINE = 6
 FAME_OPT_REFINE_TOL = 7
 FAME_OPT_PI_TABLE = 8
+FAME_OPT_C64_ROUND = 9
 FAME_SHAPE_WOODPILE, FAME_SHAPE_SPHERE, FAME_SHAPE_TETRA = 0, 1, 2
 FAME_RASTER_PAINT = 2
 
@@ -77,6 +78,8 @@ SIGNATURES = {
     "fame_restore": (_i, [_vp, _i, _pi, _vp, _pd, _vp, _vp, _pd, _pd, _pd, _i]),
     "fame_autotune": (_i, [_vp, _i, _i, _pi, _pi, _pd]),
     "fame_set_tune": (_i, [_vp, _i, _i, _i, _i]),
+    "fame_set_tune_lanes": (_i, [_vp, _i, _i, _i]),
+    "fame_get_tune": (_i, [_vp, _i, _i, _pi, _pi, _pi]),
     "fame_rasterize": (_i, [_i, _pd, _i, _pd, _i, _vp, _i]),
 }
 

@@ -41,7 +41,7 @@ def band_structure(n=60, wave_vecs=None, bands=8, gamma=0.2, eps_in=13.0, width=
     kv = band_path() if wave_vecs is None else np.atleast_2d(np.asarray(wave_vecs, dtype=np.float64))
     nk = kv.shape[0]
     if inner_tol is None:
-        inner_tol = 1e-11 if prec == "c64" else 1e-12
+        inner_tol = 3e-12 if prec == "c64" else 1e-12
     if p is None:
         p = 2 * bands + 4 if prec == "c64" else 2 * bands
     freq = np.zeros((bands, nk))
@@ -63,7 +63,7 @@ def band_structure(n=60, wave_vecs=None, bands=8, gamma=0.2, eps_in=13.0, width=
                 if tune is None:
                     tune = plan.autotune(nvec=len(idx), prec="c64")
                 else:
-                    plan.set_tune("c64", len(idx), tune["chunk"], tune["stencil_tpb"])
+                    plan.set_tune("c64", len(idx), tune["chunk"], tune["stencil_tpb"], tune.get("lanes", -1))
             r = plan.band_solve(bands, tol=tol, p=p, prec=prec, inner_tol=inner_tol, want_vectors=orgsep)
             if orgsep:
                 ev = r["ev"]

@@ -207,13 +207,14 @@ class Plan:
         check(self._lib.fame_sync(self._h), self._h, "fame_sync")
 
     def set_option(self, option, value):
-        """fame_set_option: 'precond' (bool), 'tol32' (float), 'graph' (bool), 'itol_floor' (float),
-        'plane_split' (bool), 'sira_nearest' (bool), 'refine' (bool), 'refine_tol' (float) or
-        'pi_table' (bool)."""
+        """fame_set_option: 'precond' (bool), 'tol32' (float), 'graph' (0, 1 or 2), 'itol_floor' (float),
+        'plane_split' (bool), 'sira_nearest' (bool), 'refine' (bool), 'refine_tol' (float),
+        'pi_table' (bool) or 'c64_round' (bool)."""
         code = {"precond": L.FAME_OPT_PRECOND, "tol32": L.FAME_OPT_TOL32, "graph": L.FAME_OPT_GRAPH,
                 "itol_floor": L.FAME_OPT_ITOL_FLOOR, "plane_split": L.FAME_OPT_PLANE_SPLIT,
                 "sira_nearest": L.FAME_OPT_SIRA_NEAREST, "refine": L.FAME_OPT_REFINE,
-                "refine_tol": L.FAME_OPT_REFINE_TOL, "pi_table": L.FAME_OPT_PI_TABLE}.get(option, option)
+                "refine_tol": L.FAME_OPT_REFINE_TOL, "pi_table": L.FAME_OPT_PI_TABLE,
+                "c64_round": L.FAME_OPT_C64_ROUND}.get(option, option)
         check(self._lib.fame_set_option(self._h, int(code), float(value)), self._h, "fame_set_option")
         return self
 
@@ -222,7 +223,8 @@ class Plan:
         count).  With `cache` (a JSON file path) a setting measured before on
         the same device, grid, precision and width is installed without
         re-timing, and new measurements are added to the file.
-        Returns dict(chunk, stencil_tpb, us, cached)."""
+        Returns dict(chunk, stencil_tpb, lanes, us, cached) (lanes: threads
+        per FFT pencil of the plane kernels, -1 the size's default)."""
         import json
         import os
         nvec = self.nk if nvec is None else int(nvec)
@@ -235,14 +237,14 @@ class Plan:
                 table = json.load(f)
         if key in table:
             t = table[key]
-            check(self._lib.fame_set_tune(self._h, pr, nvec, int(t["chunk"]), int(t["stencil_tpb"])), self._h,
-                  "fame_set_tune")
+            self.set_tune(pr, nvec, t["chunk"], t["stencil_tpb"], t.get("lanes", -1))
             return dict(t, cached=True)
-        ch, tpb, us = C.c_int(), C.c_int(), C.c_double()
+        ch, tpb, us, ln = C.c_int(), C.c_int(), C.c_double(), C.c_int()
         self._stream()
         check(self._lib.fame_autotune(self._h, pr, nvec, C.byref(ch), C.byref(tpb), C.byref(us)), self._h,
               "fame_autotune")
-        t = dict(chunk=ch.value, stencil_tpb=tpb.value, us=us.value)
+        check(self._lib.fame_get_tune(self._h, pr, nvec, None, None, C.byref(ln)), self._h, "fame_get_tune")
+        t = dict(chunk=ch.value, stencil_tpb=tpb.value, lanes=ln.value, us=us.value)
         if cache:
             table[key] = t
             tmp = cache + ".tmp"
@@ -251,12 +253,22 @@ class Plan:
             os.replace(tmp, cache)
         return dict(t, cached=False)
 
-    def set_tune(self, prec, nvec, chunk, stencil_tpb):
-        """fame_set_tune: install fncB launch parameters measured before (on
-        another plan of the same grid, precision and batch width)."""
+    def set_tune(self, prec, nvec, chunk, stencil_tpb, lanes=-1):
+        """fame_set_tune + fame_set_tune_lanes: install fncB launch parameters
+        measured before (on another plan of the same grid, precision and
+        batch width)."""
         pr = L.FAME_C64 if prec in ("c64", L.FAME_C64) else L.FAME_C128
         check(self._lib.fame_set_tune(self._h, pr, int(nvec), int(chunk), int(stencil_tpb)), self._h,
               "fame_set_tune")
+        check(self._lib.fame_set_tune_lanes(self._h, pr, int(nvec), int(lanes)), self._h, "fame_set_tune_lanes")
+
+    def get_tune(self, prec, nvec):
+        """fame_get_tune: the installed dict(chunk, stencil_tpb, lanes)."""
+        pr = L.FAME_C64 if prec in ("c64", L.FAME_C64) else L.FAME_C128
+        ch, tpb, ln = C.c_int(), C.c_int(), C.c_int()
+        check(self._lib.fame_get_tune(self._h, pr, int(nvec), C.byref(ch), C.byref(tpb), C.byref(ln)), self._h,
+              "fame_get_tune")
+        return dict(chunk=ch.value, stencil_tpb=tpb.value, lanes=ln.value)
 
     # -- generic call -------------------------------------------------------
     def _call(self, fn, x, out_len, inst, *extra, name=""):

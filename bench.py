@@ -7,11 +7,13 @@ xi = -zeta = 0.2i inside, vacuum outside), the 40-point band path
 Gamma-X-U|K-Gamma-L-W-X, 10 bands per k-point, every eigenpair checked with
 FP64 matvecs to the reference's
 NFSEP residual ||B x - omega A x|| <= 1e-8 for the B-normalised eigenvector x
-(fun_no_inv/EvaluteError_Chiral_no_inv.m:20).  A step solves one batch of `--batch` k-points of the path
-in one batched band solve (complex64 matvecs and inner CG, FP64 Lanczos
-recurrence, reorthogonalisation, inner-solve residual refinement, a final
-FP64 refinement sweep of every Ritz pair and the FP64 Ritz check); four
-steps of 10 cover the whole path.
+(fun_no_inv/EvaluteError_Chiral_no_inv.m:20).  A step solves `--concurrent`
+batches of `--batch` k-points of the path, each in one batched band solve
+(complex64 matvecs and inner CG, FP64 Lanczos recurrence,
+reorthogonalisation, inner-solve residual refinement, a final FP64
+refinement sweep of every Ritz pair and the FP64 Ritz check) on its own
+stream and host thread; with the defaults (2 batches of 10) two steps cover
+the whole path.
 
 Prints one JSON line (rank 0).  `--impl reference` times the reference's
 algorithm on the host cores instead (the FP64 CPU restatement; MATLAB is not
@@ -43,16 +45,17 @@ BANDS = 10
 LANCZOS_TOL = 1e-10        # the reference's Lanczos tolerance (plain FP64 form)
 # Mixed form: the Lanczos stops at 1e-8 and the final FP64 refinement sweep
 # (FAME_OPT_REFINE) polishes every Ritz pair; the bar is the NFSEP residual
-# <= 1e-8 of every pair.  Measured at n = 60 on the path's batches: worst
-# residual 2.9e-9 after the sweep (4.1e-9 before), eigenvalues within 2e-10 of
-# the FP64 form; 3-7 % faster per batch than tol 1e-10.
+# <= 1e-8 of every pair.  Lanczos tolerance 1e-10 instead takes ~10 % more
+# steps and leaves the same worst residual: below ~1e-8 the residual is set by
+# the accuracy of the inner solves, not by the Lanczos test.
 LANCZOS_TOL_MIXED = 1e-8
 INNER_TOL = 1e-12          # B^{-1} of the plain FP64 form (the reference's pcg tolerance)
-INNER_TOL_MIXED = 1e-11    # B^{-1} of the mixed form (complex64 CG + FP64 residual refinement;
+INNER_TOL_MIXED = 3e-12    # B^{-1} of the mixed form (complex64 CG + FP64 residual refinement;
                            # tightened per k-point by the Ritz-value spread, see solvers.cu).
-                           # Two complex64 rounds reach it with one FP64 residual; 1e-12 needs a
-                           # third round.  Measured at n = 60: residuals <= 2e-9 (bar 1e-8),
-                           # eigenvalues within 5e-10 of the FP64 form (reported per run).
+                           # Measured at n = 60 on the last path batch (X end): 1e-11 leaves
+                           # NFSEP residuals up to 7.5e-9, 3e-12 up to 1.8e-9 (most below
+                           # 1e-12) for 3.5 % more time; 1e-12 gives the same residuals as
+                           # 3e-12 for 24 % more time.
 # Lanczos restart size of the mixed form.  The reference uses p = 2k
 # (Computational_settings_Lanczos.m:30), which the plain FP64 sample keeps.
 # More columns cut the restarts at the batches holding Gamma, whose two
@@ -109,11 +112,12 @@ def profile_traffic():
 
 
 class Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    """nvidia-smi sampling of SM clocks, throttle reasons and utilization
+    (the share of time a kernel was running) during a region."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, gpu):
         self.gpu = gpu
@@ -138,7 +142,7 @@ class Clocks:
         except Exception:
             self.proc.kill()
         self.f.close()
-        sm, mx, reasons = [], [], set()
+        sm, mx, busy, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             parts = [p.strip() for p in line.split(",")]
@@ -152,9 +156,15 @@ class Clocks:
             for nm, v in zip(names, parts[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
+            if len(parts) > 9:
+                try:
+                    busy.append(float(parts[9]))
+                except ValueError:
+                    pass
         os.remove(self.path)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "samples": len(sm), "reasons": sorted(reasons)}
+                "samples": len(sm), "reasons": sorted(reasons),
+                "gpu_busy_pct": round(statistics.mean(busy), 1) if busy else None}
 
 
 def workload_config(batch):
@@ -219,9 +229,7 @@ def run_fame(args):
 
     def set_tune(pl):
         for pr, t in ((1, tune), (0, tune128)):
-            rc = lib.fame_set_tune(pl.raw, pr, args.batch, int(t["chunk"]), int(t["stencil_tpb"]))
-            if rc != 0:
-                raise RuntimeError("fame_set_tune failed")
+            pl.set_tune(pr, args.batch, int(t["chunk"]), int(t["stencil_tpb"]), int(t.get("lanes", -1)))
 
     for pl in plans.values():
         set_tune(pl)
@@ -427,8 +435,8 @@ def run_fame(args):
             "config": dict(workload_config(args.batch * C), batches_at_once=C, kpoints_per_batch=args.batch,
                            lanczos_p=args.lanczos_p, lanczos_tol_mixed=args.lanczos_tol,
                            batching="consecutive path points, the two Gamma points in one batch",
-                           fncb_tune={"chunk": int(tune["chunk"]), "stencil_tpb": int(tune["stencil_tpb"])},
-                           fncb_tune_c128={"chunk": int(tune128["chunk"]), "stencil_tpb": int(tune128["stencil_tpb"])},
+                           fncb_tune={k: int(tune[k]) for k in ("chunk", "stencil_tpb", "lanes")},
+                           fncb_tune_c128={k: int(tune128[k]) for k in ("chunk", "stencil_tpb", "lanes")},
                            precision="complex64 fncB + preconditioned CG, FP64 recurrence/reorth/residual "
                                      f"refinement (B^-1 to {INNER_TOL_MIXED:g}, tighter near Gamma), FP64 "
                                      "Rayleigh-Ritz refinement sweep of every Ritz pair, FP64 NFSEP check",
@@ -569,7 +577,7 @@ def profile_fncb(nvec, prec, tune=None):
     path = fame.band_path(npts=PATH_POINTS)
     plan = fame.woodpile_plan(N_GRID, path[np.arange(nvec) % len(path)])
     if tune is not None:
-        plan.set_tune(prec, nvec, tune[0], tune[1])
+        plan.set_tune(prec, nvec, tune[0], tune[1], tune[2] if len(tune) > 2 else -1)
     dt = torch.complex64 if prec == "c64" else torch.complex128
     x = torch.randn(nvec, 4 * N_GRID ** 3, dtype=dt, device="cuda")
     for _ in range(3):
@@ -608,8 +616,10 @@ def main():
                     help="k-points per step (batched band solve); 10 = the 40-point path in four steps, whose "
                          "fncB runs as two sub-batches of 5 vectors (fills the last wave of plane-kernel CTAs)")
     ap.add_argument("--impl", choices=["fame", "reference"], default="fame")
-    ap.add_argument("--concurrent", type=int, default=1,
-                    help="batches solved at once per step, each on its own stream and host thread")
+    ap.add_argument("--concurrent", type=int, default=2,
+                    help="batches solved at once per step, each on its own stream and host thread "
+                         "(2: the four path batches in two steps; measured at n = 60: 1 -> 1.90, "
+                         "2 -> 2.12, 3 -> 2.20, 4 -> 2.19 k-point solves/s, GPU busy 97.6 -> 99.5 %%)")
     ap.add_argument("--lanczos-tol", type=float, default=LANCZOS_TOL_MIXED,
                     help="Lanczos tolerance of the mixed form (the FP64 form keeps the reference's 1e-10)")
     ap.add_argument("--lanczos-p", type=int, default=LANCZOS_P_MIXED,
@@ -627,8 +637,9 @@ def main():
     ap.add_argument("--profile-fncb", type=int, default=0, metavar="NVEC",
                     help="only apply fncB three times to NVEC vectors (for ncu captures) and exit")
     ap.add_argument("--profile-prec", choices=["c64", "c128"], default="c64")
-    ap.add_argument("--profile-tune", default=None, metavar="CHUNK,TPB",
-                    help="with --profile-fncb: vectors per launch sequence and stencil threads per block")
+    ap.add_argument("--profile-tune", default=None, metavar="CHUNK,TPB[,LANES]",
+                    help="with --profile-fncb: vectors per launch sequence, stencil threads per block and "
+                         "threads per FFT pencil of the plane kernels (-1 default, 0 one)")
     ap.add_argument("--profile-cg", type=int, default=0, metavar="NVEC",
                     help="only run two 4-iteration complex64 CG solves on NVEC vectors (for ncu) and exit")
     args = ap.parse_args()

@@ -80,8 +80,14 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *                     unpreconditioned pcg of fncinvB.m.
  *   FAME_OPT_TOL32    complex64 CG tolerance of the first refinement round of
  *                     the mixed-precision B^{-1} [1e-6].
- *   FAME_OPT_GRAPH    replay blocks of CG iterations from CUDA graphs captured
- *                     on first use [1]; 0 launches every kernel directly.
+ *   FAME_OPT_GRAPH    CG iterations from CUDA graphs captured on first use:
+ *                     2 the whole iteration loop in one graph launch (blocks
+ *                     of four iterations in a conditional WHILE node whose
+ *                     condition, any vector still active, is set on the
+ *                     device; the host waits once per solve) [2]; 1 one graph
+ *                     launch per block of four iterations with a host-side
+ *                     convergence check after each; 0 every kernel launched
+ *                     directly.  All three give the same iterates.
  *   FAME_OPT_ITOL_FLOOR  mixed form: lower bound of the per-instance inner
  *                     tolerance, which is tightened by the spread of the
  *                     wanted Ritz values and starts there at near-zero wave
@@ -104,10 +110,15 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *   FAME_OPT_PI_TABLE  complex128 fncB reads the per-voxel Pi blocks from the
  *                     table the plan builds at creation (96 B per voxel and
  *                     k-point) [1]; 0 evaluates them in the transform kernels
- *                     (same values to rounding).  Complex64 always evaluates. */
+ *                     (same values to rounding).  Complex64 always evaluates.
+ *   FAME_OPT_C64_ROUND  mixed B^{-1}: the second refinement round updates
+ *                     B x with a complex64 apply of its correction [1]
+ *                     (estimates the residual to ~1e-11 of b); 0 takes an
+ *                     FP64 apply in every round (B x exact after each). */
 enum fame_option {
   FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2, FAME_OPT_ITOL_FLOOR = 3, FAME_OPT_PLANE_SPLIT = 4,
-  FAME_OPT_SIRA_NEAREST = 5, FAME_OPT_REFINE = 6, FAME_OPT_REFINE_TOL = 7, FAME_OPT_PI_TABLE = 8
+  FAME_OPT_SIRA_NEAREST = 5, FAME_OPT_REFINE = 6, FAME_OPT_REFINE_TOL = 7, FAME_OPT_PI_TABLE = 8,
+  FAME_OPT_C64_ROUND = 9
 };
 int fame_set_option(fame_plan_t plan, int option, double value);
 
@@ -123,13 +134,20 @@ int fame_refine_residuals(fame_plan_t plan, double* before, int n);
  * fncB sequence for precision `prec` and batch width `nvec` on this plan
  * (vectors per launch sequence: the whole batch, 1/2, 1/4, 1/8 of it or any
  * width up to 16; the material stencil: 0 = single pass, or 128, 256, 512
- * threads per block of the two-kernel form) and keep the
- * fastest for later calls with that width.  Outputs (may be NULL): the chosen
- * chunk (0 = whole batch), stencil setting and the measured microseconds of
- * one fncB.  fame_set_tune installs a setting directly (e.g. from a cache).
+ * threads per block of the two-kernel form; the plane kernels' split of each
+ * FFT pencil: threads per pencil, every count compiled for the grid size, or
+ * one) and keep the fastest for later calls with that width.  Outputs (may be
+ * NULL): the chosen chunk (0 = whole batch), stencil setting and the measured
+ * microseconds of one fncB.  fame_set_tune installs a chunk and stencil
+ * setting directly (e.g. from a cache), keeping the width's split;
+ * fame_set_tune_lanes installs the split (-1 = the size's default, 0 = one
+ * thread per pencil, else a compiled count; others fall back to the
+ * default); fame_get_tune reads the installed setting (lanes -1 = default).
  */
 int fame_autotune(fame_plan_t plan, int prec, int nvec, int* chunk, int* stencil_tpb, double* us);
 int fame_set_tune(fame_plan_t plan, int prec, int nvec, int chunk, int stencil_tpb);
+int fame_set_tune_lanes(fame_plan_t plan, int prec, int nvec, int lanes);
+int fame_get_tune(fame_plan_t plan, int prec, int nvec, int* chunk, int* stencil_tpb, int* lanes);
 int fame_sync(fame_plan_t plan);
 const char* fame_last_error(fame_plan_t plan);
 int fame_plan_info(fame_plan_t plan, int* n, int* nk, long long* nq);

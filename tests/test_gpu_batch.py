@@ -53,3 +53,35 @@ def test_autotuned_fncB_unchanged(cuda, fame_lib, dtype):
     tol = 1e-6 if dtype == "c64" else 1e-14
     d = torch.linalg.norm(ref["sweep"] - ref["two-kernel"]) / torch.linalg.norm(ref["two-kernel"])
     assert float(d) < tol
+
+
+@pytest.mark.parametrize("dtype", ["c64", "c128"])
+def test_plane_lanes_give_the_same_fncB(cuda, fame_lib, dtype):
+    """The plane kernels' split of each FFT pencil (threads per pencil: the
+    prime-factor splits 60 = 3*20, 4*15, 5*12 compiled at n = 60, or one
+    thread per pencil) changes how the DFTs are evaluated, not the operator:
+    every lane count agrees with the default to rounding, an unknown count
+    falls back to the default bit for bit, and the autotuner reports a
+    compiled choice."""
+    n = 60
+    plan = fame.woodpile_plan(n, fame.band_path(npts=40)[:2])
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((2, 4 * n ** 3)) + 1j * rng.standard_normal((2, 4 * n ** 3))
+    xt = torch.as_tensor(x).to(torch.complex64 if dtype == "c64" else torch.complex128).cuda()
+    plan.set_tune(dtype, 2, 0, 0 if dtype == "c64" else 256, -1)
+    ref = plan.apply_B(xt)
+    assert plan.get_tune(dtype, 2)["lanes"] == -1
+    tol = 2e-6 if dtype == "c64" else 1e-13
+    for lanes in (0, 3, 4, 5):
+        plan.set_tune(dtype, 2, 0, 0 if dtype == "c64" else 256, lanes)
+        assert plan.get_tune(dtype, 2)["lanes"] == lanes
+        y = plan.apply_B(xt)
+        d = float(torch.linalg.norm(y - ref) / torch.linalg.norm(ref))
+        assert d < tol, (lanes, d)
+        if lanes == 3:
+            assert torch.equal(y, ref)  # 3 is the default at n = 60
+    plan.set_tune(dtype, 2, 0, 0 if dtype == "c64" else 256, 7)  # not compiled: the default
+    assert torch.equal(plan.apply_B(xt), ref)
+    t = plan.autotune(nvec=2, prec=dtype)
+    assert t["lanes"] in (-1, 0, 3, 4, 5)
+    plan.close()

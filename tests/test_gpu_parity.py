@@ -163,8 +163,10 @@ def test_errors(cuda, fame_lib):
 
 @pytest.mark.parametrize("prec", ["c128", "c64"])
 def test_cg_graph_replay_matches_direct_launches(cuda, fame_lib, prec):
-    """Blocks of CG iterations replayed from captured CUDA graphs give the same
-    iterates as launching every kernel directly (same kernels, same order)."""
+    """The CG loop replayed from one graph launch (device-side loop
+    condition), blocks of CG iterations replayed from captured CUDA graphs,
+    and every kernel launched directly give the same iterates (same kernels,
+    same order)."""
     pr = Pair(8, nk=2, seed=21)
     rng = np.random.default_rng(5)
     b = rng.standard_normal((3, 4 * pr.Nq)) + 1j * rng.standard_normal((3, 4 * pr.Nq))
@@ -172,12 +174,13 @@ def test_cg_graph_replay_matches_direct_launches(cuda, fame_lib, prec):
     bt = torch.as_tensor(b).to(torch.complex128 if prec == "c128" else torch.complex64).cuda()
     tol = 1e-10 if prec == "c128" else 1e-5
     out = {}
-    for g in (1, 0):
+    for g in (2, 1, 0):
         pr.plan.set_option("graph", g)
         y, its, rr = pr.plan.apply_Binv(bt, tol=tol, maxit=2000)
         y2, its2, _ = pr.plan.apply_Binv(bt, tol=tol, maxit=2000)
         assert torch.equal(y, y2) and np.array_equal(its, its2)  # second call replays the cached graph
         out[g] = (y.cpu().numpy(), its.copy(), rr.copy())
-    pr.plan.set_option("graph", 1)
-    assert np.array_equal(out[1][1], out[0][1])
-    assert np.array_equal(out[1][0], out[0][0])
+    pr.plan.set_option("graph", 2)
+    for g in (2, 1):
+        assert np.array_equal(out[g][1], out[0][1])
+        assert np.array_equal(out[g][0], out[0][0])

@@ -44,3 +44,20 @@ def test_refinement_keeps_eigenvalues_and_lowers_residuals(cuda, fame_lib):
     # per-instance counts: the sweep adds at least 2k FP64 applies per instance
     assert np.all(ref_m["stats"][:, 2] >= raw["stats"][:, 2] + 2 * k)
     plan.close()
+
+
+@pytest.mark.parametrize("refine_tol", [1e-9, 1e-12])
+def test_refinement_with_tight_search_solve(cuda, fame_lib, refine_tol):
+    """The sweep's search directions W = B^-1 R solved far below the size of
+    the residuals R (~1e-10 and less): every complex64 round of the mixed
+    solve sees a right-hand side scaled to norm [1, 2), so no CG product
+    underflows and the band solve completes with residuals no larger than
+    before the sweep."""
+    n, k = 12, 6
+    plan = fame.woodpile_plan(n, [fame.fcc_point("X"), fame.fcc_point("L")])
+    plan.set_option("refine_tol", refine_tol)
+    m = plan.band_solve(k, tol=1e-8, prec="c64", inner_tol=3e-12, p=2 * k + 4)
+    assert m["status"] == 0
+    assert np.all(m["res"] <= m["res_before"])
+    assert m["res"].max() <= 1e-8
+    plan.close()

@@ -17,10 +17,10 @@ class FakePlan:
 
     def autotune(self, nvec=None, prec="c64"):
         self.tuned = ("auto", nvec)
-        return {"chunk": 2, "stencil_tpb": 128}
+        return {"chunk": 2, "stencil_tpb": 128, "lanes": 4}
 
-    def set_tune(self, prec, nvec, chunk, tpb):
-        self.tuned = ("set", nvec, chunk, tpb)
+    def set_tune(self, prec, nvec, chunk, tpb, lanes=-1):
+        self.tuned = ("set", nvec, chunk, tpb, lanes)
 
     def band_solve(self, k, tol, p, prec, inner_tol, want_vectors):
         key = self.kv[:, 0][:, None]  # first wave-vector component identifies the k-point
@@ -49,7 +49,7 @@ def test_batches_map_back_to_path_order(monkeypatch, tmp_path):
     assert [p.nk for p in FakePlan.made] == [3, 3, 1]
     assert all(p.closed for p in FakePlan.made)
     assert FakePlan.made[0].tuned == ("auto", 3)
-    assert FakePlan.made[1].tuned == ("set", 3, 2, 128)
+    assert FakePlan.made[1].tuned == ("set", 3, 2, 128, 4)
     expect = (np.arange(7) + 1.0)[None, :] + np.arange(4)[:, None] / 100.0
     assert np.allclose(r["Freq_mtx"], expect)
     assert np.allclose(r["res_ORGSEP"], expect * 1e-9)
