@@ -362,6 +362,10 @@ int fame_set_option(fame_plan_t h, int option, double value) {
     case FAME_OPT_C64_ROUND:
       P.opt_c64_round = value != 0.0;
       return FAME_OK;
+    case FAME_OPT_RELAX:
+      if (!(value >= 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: relax must be in [0, 1)");
+      P.opt_relax = value;
+      return FAME_OK;
     case FAME_OPT_REFINE_TOL:
       if (!(value > 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: refine tol in (0, 1)");
       P.opt_refine_tol = value;

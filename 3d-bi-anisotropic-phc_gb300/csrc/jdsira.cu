@@ -166,6 +166,7 @@ int minres_shifted(Plan& P, const cx<R>* b, cx<R>* x, const int* d_inst, double 
   cx<R> *v = base, *y = base + L, *r1 = base + 2 * L, *r2 = base + 3 * L, *w = base + 4 * L, *w1 = base + 5 * L,
         *w2 = base + 6 * L, *ta = base + 7 * L;
   char* sm = (char*)workspace(P, JD_R32 + 30, sizeof(double2) * (3 * 256 + 8) + sizeof(double) * MR_NSLOT + 64, &e);
+  static_assert(sizeof(MrInt) + sizeof(int) <= 64, "loop pass counter after the integer state");
   JD_CK(e, "minres workspace");
   double2* part = (double2*)sm;          // dot partials
   double2* dalfa = part + 256;           // v . y
@@ -265,7 +266,35 @@ int minres_shifted(Plan& P, const cx<R>* b, cx<R>* x, const int* d_inst, double 
   MrInt hst = hi;
   double phibar = beta1;
   int done_steps = 0;
-  while (done_steps < maxit) {
+  if (P.opt_graph >= 2 && maxit >= kMinresBlock) {
+    // all blocks of kMinresBlock steps in one graph launch, the stopping
+    // test on the device after each block; the host waits once
+    int* passes = (int*)(SI + 1);
+    std::vector<uintptr_t> wkey = gkey;
+    wkey.push_back((uintptr_t)0x5748494cu);
+    wkey.push_back((uintptr_t)(maxit / kMinresBlock));
+    unsigned long long body_nodes = 0;
+    cudaError_t ge = graph_replay_while(P, wkey, [&](cudaStream_t cs) -> cudaError_t {
+      for (int i = 0; i < kMinresBlock; ++i) {
+        cudaError_t e2 = step(cs);
+        if (e2 != cudaSuccess) return e2;
+      }
+      return cudaSuccess;
+    }, &SI->active, 1, passes, maxit / kMinresBlock, &body_nodes);
+    if (ge == cudaSuccess) {
+      int np = 0;
+      JD_CK(cudaMemcpyAsync(&hst, SI, sizeof(MrInt), cudaMemcpyDeviceToHost, st), "minres check");
+      JD_CK(cudaMemcpyAsync(&phibar, S + MR_PHIBAR, sizeof(double), cudaMemcpyDeviceToHost, st), "minres check");
+      JD_CK(cudaMemcpyAsync(&np, passes, sizeof(int), cudaMemcpyDeviceToHost, st), "minres check");
+      JD_CK(cudaStreamSynchronize(st), "minres check");
+      FAME_LAUNCHED(body_nodes * (unsigned long long)np);
+      done_steps = np * kMinresBlock;
+      if (hst.nan) return fail(&P, FAME_ERR_NAN, "minres: non-finite value");
+    } else if (ge != cudaErrorNotSupported) {
+      JD_CK(ge, "minres graph loop");
+    }
+  }
+  while (done_steps < maxit && hst.active) {
     const int nb = std::min(kMinresBlock, maxit - done_steps);
     bool issued = false;
     if (use_graph && nb == kMinresBlock) {

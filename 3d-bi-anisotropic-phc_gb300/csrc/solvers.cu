@@ -1071,9 +1071,12 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
       std::iota(ind.begin(), ind.end(), 0);
       std::stable_sort(ind.begin(), ind.end(), [&](int x, int y) { return w[x] > w[y]; });  // :109
       int nconv = 0;
+      double rel_max = 0.0;  // largest relative Ritz residual of the wanted pairs
       for (int i = 0; i < I.k0; ++i) {
         const double resi = std::fabs(I.beta * Uv[(size_t)ind[i] * np + np - 1]);  // :106
-        if (resi < tol * std::max(std::pow(eps, 2.0 / 3.0), std::fabs(w[ind[i]]))) nconv++;  // :114
+        const double scale = std::max(std::pow(eps, 2.0 / 3.0), std::fabs(w[ind[i]]));
+        if (resi < tol * scale) nconv++;  // :114
+        rel_max = std::max(rel_max, resi / scale);
       }
       if (nconv >= I.k0 || I.mm == maxit) {  // :117
         if (nconv < I.k0) rc_final = FAME_ERR_NOT_CONVERGED;
@@ -1094,6 +1097,13 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         const double lmax = std::fabs(w[ind[0]]), lk = std::fabs(w[ind[I.k0 - 1]]);
         const double spread = lmax > 0.0 ? std::min(1.0, lk / lmax) : 1.0;
         I.itol = std::max(P.opt_itol_floor, itol * spread);
+        // Relaxed inner accuracy (FAME_OPT_RELAX = c > 0): once every wanted
+        // Ritz pair's relative residual is below c, the error a new Lanczos
+        // vector carries enters the wanted pairs with a weight of about that
+        // residual, so the inner tolerance may grow by c / residual (at most
+        // 1e3); no relaxation for the Gamma-like instances at the floor.
+        if (P.opt_relax > 0.0 && !I.explicit_br && rel_max > 0.0)
+          I.itol *= std::min(1e3, std::max(1.0, P.opt_relax / rel_max));
         I.refresh_bq = !I.explicit_br && spread < 1e-3;
         I.explicit_br = spread < 1e-3;
       }

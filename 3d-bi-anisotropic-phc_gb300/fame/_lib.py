@@ -35,6 +35,7 @@ FAME_OPT_REFINE = 6
 FAME_OPT_REFINE_TOL = 7
 FAME_OPT_PI_TABLE = 8
 FAME_OPT_C64_ROUND = 9
+FAME_OPT_RELAX = 10
 FAME_SHAPE_WOODPILE, FAME_SHAPE_SPHERE, FAME_SHAPE_TETRA = 0, 1, 2
 FAME_RASTER_PAINT = 2
 

@@ -50,3 +50,23 @@ def test_jdsira_matches_dense_spectrum(cuda, fame_lib, target, gamma, inner_prec
     au = plan.apply_A(ev).cpu().numpy()
     for i in range(nev):
         assert np.linalg.norm(bu[i] - r["ew"][i] * au[i]) < 1e-7
+
+
+def test_jdsira_graph_modes_agree(cuda, fame_lib):
+    """The shifted MINRES of the correction equation run as one graph launch
+    per solve (device-side stopping test), as one launch per block of steps
+    with a host check, and launched kernel by kernel: the same iterates, so
+    the same eigenpairs to the last bit."""
+    n, nev, target = 4, 3, 6.0
+    kvec = fame.fcc_point("X")
+    out = {}
+    for g in (2, 1, 0):
+        plan = fame.woodpile_plan(n, [kvec], gamma=0.5)
+        plan.set_option("graph", g)
+        r = plan.jdsira(nev, target=target, tol=1e-8, no_restart=30, restart_dim=4, inner_tol=1e-2,
+                        inner_prec="c128", want_vectors=False, shift=target)
+        assert r["status"] == 0
+        out[g] = (np.asarray(r["ew"]), np.asarray(r["res"]))
+        plan.close()
+    for g in (2, 1):
+        assert np.array_equal(out[g][0], out[0][0]) and np.array_equal(out[g][1], out[0][1])
