@@ -115,12 +115,14 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *                     B x with a complex64 apply of its correction [1]
  *                     (estimates the residual to ~1e-11 of b); 0 takes an
  *                     FP64 apply in every round (B x exact after each).
- *   FAME_OPT_RELAX    mixed Lanczos: c in [0, 1) [0 = off].  At a restart
- *                     where every wanted Ritz pair's relative residual r is
- *                     below c, the instance's inner tolerance is multiplied by
- *                     min(1e3, c / max r) (relaxed inner accuracy for the
- *                     late Lanczos vectors, which enter the wanted pairs with
- *                     a weight of about r). */
+ *   FAME_OPT_RELAX    mixed Lanczos: c in [0, 1) [0.1; 0 = off].  At a
+ *                     restart where every wanted Ritz pair's relative
+ *                     residual r is below c, the instance's inner tolerance is
+ *                     multiplied by min(1e3, c / max r) (relaxed inner
+ *                     accuracy for the late Lanczos vectors, which enter the
+ *                     wanted pairs with a weight of about r).  The
+ *                     Gamma-like instances at the tolerance floor are not
+ *                     relaxed. */
 enum fame_option {
   FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2, FAME_OPT_ITOL_FLOOR = 3, FAME_OPT_PLANE_SPLIT = 4,
   FAME_OPT_SIRA_NEAREST = 5, FAME_OPT_REFINE = 6, FAME_OPT_REFINE_TOL = 7, FAME_OPT_PI_TABLE = 8,

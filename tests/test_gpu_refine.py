@@ -61,3 +61,28 @@ def test_refinement_with_tight_search_solve(cuda, fame_lib, refine_tol):
     assert np.all(m["res"] <= m["res_before"])
     assert m["res"].max() <= 1e-8
     plan.close()
+
+
+def test_relaxed_inner_tolerance(cuda, fame_lib):
+    """FAME_OPT_RELAX: the inner solves of the late Lanczos vectors may be
+    looser once the wanted Ritz residuals are small.  Against no relaxation:
+    about the same Lanczos steps, eigenvalues of the FP64 form to 1e-9, NFSEP
+    residuals below the bar, and no more inner CG iterations."""
+    n, k = 12, 6
+    kv = [fame.fcc_point("X"), fame.fcc_point("L")]
+    plan = fame.woodpile_plan(n, kv)
+    ref = plan.band_solve(k, tol=1e-11, prec="c128", inner_tol=1e-13, p=2 * k)
+    out = {}
+    for c in (0.0, 0.1, 0.5):
+        plan.set_option("relax", c)
+        out[c] = plan.band_solve(k, tol=1e-8, prec="c64", inner_tol=3e-12, p=2 * k + 4)
+        assert out[c]["status"] == 0
+        assert out[c]["res"].max() <= 1e-8
+        assert np.allclose(out[c]["ew"], ref["ew"], rtol=1e-9, atol=0)
+    steps0 = out[0.0]["stats"][:, 0].sum()
+    for c in (0.1, 0.5):
+        assert abs(out[c]["stats"][:, 0].sum() - steps0) <= 0.1 * steps0
+    assert out[0.5]["stats"][:, 3].sum() <= out[0.0]["stats"][:, 3].sum()
+    with pytest.raises(fame.FameError):
+        plan.set_option("relax", 1.5)
+    plan.close()

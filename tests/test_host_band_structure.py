@@ -70,3 +70,22 @@ def test_fp64_form_skips_autotune_and_orgsep(monkeypatch):
     assert FakePlan.made[0].tuned is None
     assert np.isnan(r["res_ORGSEP"]).all()
     assert r["Freq_mtx"].shape == (2, 4)
+
+
+def test_concurrent_batches_fill_the_same_arrays(monkeypatch):
+    """Batches solved on concurrent host threads land in the same places as
+    one after another; the first batch is tuned alone and the others get its
+    setting."""
+    monkeypatch.setattr(BS, "woodpile_plan", FakePlan)
+    kv = np.stack([np.array([float(i + 1), 0.0, 0.0]) for i in range(11)])
+    FakePlan.made = []
+    seq = BS.band_structure(12, kv, bands=3, batch=2, prec="c64", concurrent=1)
+    FakePlan.made = []
+    con = BS.band_structure(12, kv, bands=3, batch=2, prec="c64", concurrent=3)
+    assert sorted(p.nk for p in FakePlan.made) == [1, 2, 2, 2, 2, 2]
+    assert all(p.closed for p in FakePlan.made)
+    # one autotune per batch width (2 and the last batch's 1), the rest installed
+    assert sum(1 for p in FakePlan.made if p.tuned and p.tuned[0] == "auto") == 2
+    assert sum(1 for p in FakePlan.made if p.tuned and p.tuned[0] == "set") == 4
+    for key in ("Freq_mtx", "res_NFSEP", "res_ORGSEP", "iter_records", "cg_iterations", "status"):
+        assert np.array_equal(seq[key], con[key]), key
