@@ -366,6 +366,10 @@ int fame_set_option(fame_plan_t h, int option, double value) {
       if (!(value >= 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: relax must be in [0, 1)");
       P.opt_relax = value;
       return FAME_OK;
+    case FAME_OPT_RELAX_MAX:
+      if (!(value >= 1.0 && value <= 1e8)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: relax_max must be in [1, 1e8]");
+      P.opt_relax_max = value;
+      return FAME_OK;
     case FAME_OPT_REFINE_TOL:
       if (!(value > 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: refine tol in (0, 1)");
       P.opt_refine_tol = value;

@@ -97,7 +97,8 @@ struct Plan {
   // options (fame_set_option)
   int opt_precond = 1;                // CG on B preconditioned by the averaged-medium B0^{-1}
   double opt_tol32 = 1e-6;            // complex64 CG tolerance of the first refinement round
-  double opt_relax = 0.1;             // mixed Lanczos: relax the inner tolerance once Ritz residuals < this
+  double opt_relax = 0.5;             // mixed Lanczos: relax the inner tolerance once Ritz residuals < this
+  double opt_relax_max = 1e6;         // largest relaxation factor
   int opt_c64_round = 1;              // mixed B^{-1}: second round's B x update in complex64 (0: FP64 apply)
   int opt_graph = 2;                  // CG from CUDA graphs: 1 blocks of iterations, 2 the whole loop
   double opt_itol_floor = 1e-13;      // mixed form: floor of the spread-scaled inner tolerance

@@ -1101,9 +1101,10 @@ int lanczos_run(Plan& P, int prec, const std::vector<int>& insts, int k0, double
         // Ritz pair's relative residual is below c, the error a new Lanczos
         // vector carries enters the wanted pairs with a weight of about that
         // residual, so the inner tolerance may grow by c / residual (at most
-        // 1e3); no relaxation for the Gamma-like instances at the floor.
+        // FAME_OPT_RELAX_MAX); no relaxation for the Gamma-like instances at
+        // the floor.
         if (P.opt_relax > 0.0 && !I.explicit_br && rel_max > 0.0)
-          I.itol *= std::min(1e3, std::max(1.0, P.opt_relax / rel_max));
+          I.itol *= std::min(P.opt_relax_max, std::max(1.0, P.opt_relax / rel_max));
         I.refresh_bq = !I.explicit_br && spread < 1e-3;
         I.explicit_br = spread < 1e-3;
       }

@@ -36,6 +36,7 @@ FAME_OPT_REFINE_TOL = 7
 FAME_OPT_PI_TABLE = 8
 FAME_OPT_C64_ROUND = 9
 FAME_OPT_RELAX = 10
+FAME_OPT_RELAX_MAX = 11
 FAME_SHAPE_WOODPILE, FAME_SHAPE_SPHERE, FAME_SHAPE_TETRA = 0, 1, 2
 FAME_RASTER_PAINT = 2
 

@@ -438,8 +438,8 @@ def run_fame(args):
                            fncb_tune={k: int(tune[k]) for k in ("chunk", "stencil_tpb", "lanes")},
                            fncb_tune_c128={k: int(tune128[k]) for k in ("chunk", "stencil_tpb", "lanes")},
                            precision="complex64 fncB + preconditioned CG, FP64 recurrence/reorth/residual "
-                                     f"refinement (B^-1 to {INNER_TOL_MIXED:g}, tighter near Gamma, relaxed up to "
-                                     "1e3x for late Lanczos vectors once the Ritz residuals are < 0.1), FP64 "
+                                     f"refinement (B^-1 to {INNER_TOL_MIXED:g}, tighter near Gamma, relaxed by "
+                                     "0.5 / (largest relative Ritz residual) for later Lanczos vectors), FP64 "
                                      "Rayleigh-Ritz refinement sweep of every Ritz pair, FP64 NFSEP check",
                            l2="inputs larger than L2 (Lanczos basis and B*Q of a batch "
                               f"{2 * args.batch * args.lanczos_p * 4 * N_GRID ** 3 * 16 / 1e9:.1f} GB)"),

@@ -115,18 +115,21 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *                     B x with a complex64 apply of its correction [1]
  *                     (estimates the residual to ~1e-11 of b); 0 takes an
  *                     FP64 apply in every round (B x exact after each).
- *   FAME_OPT_RELAX    mixed Lanczos: c in [0, 1) [0.1; 0 = off].  At a
+ *   FAME_OPT_RELAX    mixed Lanczos: c in [0, 1) [0.5; 0 = off].  At a
  *                     restart where every wanted Ritz pair's relative
  *                     residual r is below c, the instance's inner tolerance is
- *                     multiplied by min(1e3, c / max r) (relaxed inner
+ *                     multiplied by min(FAME_OPT_RELAX_MAX, c / max r) (relaxed inner
  *                     accuracy for the late Lanczos vectors, which enter the
  *                     wanted pairs with a weight of about r).  The
  *                     Gamma-like instances at the tolerance floor are not
- *                     relaxed. */
+ *                     relaxed.
+ *   FAME_OPT_RELAX_MAX  the largest factor of that relaxation [1e6].  The error
+ *                     such a solve adds to a wanted pair is bounded by about
+ *                     (inner tolerance) x c whatever the factor. */
 enum fame_option {
   FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2, FAME_OPT_ITOL_FLOOR = 3, FAME_OPT_PLANE_SPLIT = 4,
   FAME_OPT_SIRA_NEAREST = 5, FAME_OPT_REFINE = 6, FAME_OPT_REFINE_TOL = 7, FAME_OPT_PI_TABLE = 8,
-  FAME_OPT_C64_ROUND = 9, FAME_OPT_RELAX = 10
+  FAME_OPT_C64_ROUND = 9, FAME_OPT_RELAX = 10, FAME_OPT_RELAX_MAX = 11
 };
 int fame_set_option(fame_plan_t plan, int option, double value);
 
