@@ -37,6 +37,7 @@ template <> PlanData<double>& pdata_mut<double>(Plan& P) { return P.d64; }
 template <> PlanData<float>& pdata_mut<float>(Plan& P) { return P.d32; }
 
 unsigned long long g_kernel_launches = 0;
+unsigned long long g_host_launches = 0;
 
 void* workspace(Plan& P, int id, size_t bytes, cudaError_t* err) {
   *err = cudaSuccess;
@@ -236,6 +237,7 @@ extern "C" {
 const char* fame_version(void) { return "fame-gb300 0.1 (sm_103a)"; }
 
 long long fame_kernel_launches(void) { return (long long)__atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED); }
+long long fame_host_launches(void) { return (long long)__atomic_load_n(&g_host_launches, __ATOMIC_RELAXED); }
 
 int fame_plan_create(fame_plan_t* out, int n, int nk, const double* theta, const uint8_t* phase, int nphase,
                      const double* tensors) {

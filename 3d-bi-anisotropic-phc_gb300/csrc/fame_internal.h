@@ -13,9 +13,25 @@
 
 namespace fame {
 
-// Number of kernels this library has launched (all plans, all threads).
+// Kernels this library has run (all plans, all threads), and the launch
+// calls it made from the host for them (a graph launch counts once however
+// many kernels it runs).
 extern unsigned long long g_kernel_launches;
-#define FAME_LAUNCHED(n) __atomic_fetch_add(&::fame::g_kernel_launches, (unsigned long long)(n), __ATOMIC_RELAXED)
+extern unsigned long long g_host_launches;
+// n kernels launched directly
+#define FAME_LAUNCHED(n)                                                                              \
+  (__atomic_fetch_add(&::fame::g_kernel_launches, (unsigned long long)(n), __ATOMIC_RELAXED),       \
+   __atomic_fetch_add(&::fame::g_host_launches, (unsigned long long)(n), __ATOMIC_RELAXED))
+// one graph launch running `nodes` kernels
+#define FAME_GRAPH_LAUNCHED(nodes)                                                                    \
+  (__atomic_fetch_add(&::fame::g_kernel_launches, (unsigned long long)(nodes), __ATOMIC_RELAXED),   \
+   __atomic_fetch_add(&::fame::g_host_launches, 1ull, __ATOMIC_RELAXED))
+// kernels run by the loop body of a graph launch, counted once the loop ended
+#define FAME_KERNELS_RAN(n) __atomic_fetch_add(&::fame::g_kernel_launches, (unsigned long long)(n), __ATOMIC_RELAXED)
+// launches recorded by a stream capture (counted by FAME_LAUNCHED, not run)
+#define FAME_UNCOUNT_CAPTURED(n)                                                                      \
+  (__atomic_fetch_sub(&::fame::g_kernel_launches, (unsigned long long)(n), __ATOMIC_RELAXED),       \
+   __atomic_fetch_sub(&::fame::g_host_launches, (unsigned long long)(n), __ATOMIC_RELAXED))
 
 // Which vectors of a batch belong to which k-point instance, and which are
 // still active (converged vectors of a batched solve are skipped).

@@ -31,7 +31,7 @@ cudaError_t graph_replay(Plan& P, const std::vector<uintptr_t>& key, F&& issue) 
     // The graph's own kernel nodes are counted, not the counter's change,
     // which also holds other threads' launches on other plans.
     const unsigned long long captured = g ? graph_kernel_nodes(g) : 0;
-    __atomic_fetch_sub(&g_kernel_launches, captured, __ATOMIC_RELAXED);
+    FAME_UNCOUNT_CAPTURED(captured);
     if (ie != cudaSuccess || e != cudaSuccess) {
       if (g) cudaGraphDestroy(g);
       cudaGetLastError();
@@ -42,7 +42,7 @@ cudaError_t graph_replay(Plan& P, const std::vector<uintptr_t>& key, F&& issue) 
     if (e != cudaSuccess) return e;
   }
   e = cudaGraphLaunch(ge->exec, P.stream);
-  if (e == cudaSuccess) FAME_LAUNCHED(ge->nodes);
+  if (e == cudaSuccess) FAME_GRAPH_LAUNCHED(ge->nodes);
   return e;
 }
 
@@ -52,7 +52,7 @@ cudaError_t graph_replay(Plan& P, const std::vector<uintptr_t>& key, F&& issue) 
 // host neither waits nor launches between passes.  The body always runs at
 // least once.  *passes (device) counts the passes of this launch; the caller
 // reads it after the stream completes and adds passes x *body_nodes to the
-// launch count (the body's kernels are not counted here).  Cached under
+// kernel count (FAME_KERNELS_RAN; the graph launch itself is counted here).  Cached under
 // `key` like graph_replay.  Returns cudaErrorNotSupported when conditional
 // nodes or capture are unavailable (the caller falls back to graph_replay).
 template <class F>
@@ -96,7 +96,7 @@ cudaError_t graph_replay_while(Plan& P, const std::vector<uintptr_t>& key, F&& b
     e = cudaStreamEndCapture(P.cap_stream, &got);
     // recorded, not run: the body's kernels are counted per pass when replayed
     const unsigned long long captured = graph_kernel_nodes(bg);
-    __atomic_fetch_sub(&g_kernel_launches, captured, __ATOMIC_RELAXED);
+    FAME_UNCOUNT_CAPTURED(captured);
     if (ie != cudaSuccess || e != cudaSuccess) {
       cudaGraphDestroy(g);
       cudaGetLastError();
@@ -111,7 +111,10 @@ cudaError_t graph_replay_while(Plan& P, const std::vector<uintptr_t>& key, F&& b
   }
   e = cudaMemsetAsync(passes, 0, sizeof(int), P.stream);
   if (e == cudaSuccess) e = cudaGraphLaunch(ge->exec, P.stream);
-  if (e == cudaSuccess) *body_nodes = ge->nodes;
+  if (e == cudaSuccess) {
+    FAME_GRAPH_LAUNCHED(0);  // the body's kernels: FAME_KERNELS_RAN by the caller
+    *body_nodes = ge->nodes;
+  }
   return e;
 }
 

@@ -287,7 +287,7 @@ int minres_shifted(Plan& P, const cx<R>* b, cx<R>* x, const int* d_inst, double 
       JD_CK(cudaMemcpyAsync(&phibar, S + MR_PHIBAR, sizeof(double), cudaMemcpyDeviceToHost, st), "minres check");
       JD_CK(cudaMemcpyAsync(&np, passes, sizeof(int), cudaMemcpyDeviceToHost, st), "minres check");
       JD_CK(cudaStreamSynchronize(st), "minres check");
-      FAME_LAUNCHED(body_nodes * (unsigned long long)np);
+      FAME_KERNELS_RAN(body_nodes * (unsigned long long)np);
       done_steps = np * kMinresBlock;
       if (hst.nan) return fail(&P, FAME_ERR_NAN, "minres: non-finite value");
     } else if (ge != cudaErrorNotSupported) {

@@ -232,7 +232,7 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
       FAME_CK(cudaMemcpyAsync(act.data(), S.active, sizeof(int) * nvec, cudaMemcpyDeviceToHost, st), "pcg check");
       FAME_CK(cudaMemcpyAsync(&passes, S.passes, sizeof(int), cudaMemcpyDeviceToHost, st), "pcg check");
       FAME_CK(cudaStreamSynchronize(st), "pcg check");
-      FAME_LAUNCHED(body_nodes * (unsigned long long)passes);
+      FAME_KERNELS_RAN(body_nodes * (unsigned long long)passes);
       it = 1 + passes * chk;
       any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
     } else if (ge != cudaErrorNotSupported) {

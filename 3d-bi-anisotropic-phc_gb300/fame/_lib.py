@@ -55,6 +55,7 @@ _pll = C.POINTER(C.c_longlong)
 SIGNATURES = {
     "fame_version": (C.c_char_p, []),
     "fame_kernel_launches": (C.c_longlong, []),
+    "fame_host_launches": (C.c_longlong, []),
     "fame_plan_create": (_i, [C.POINTER(_vp), _i, _i, _pd, C.POINTER(C.c_uint8), _i, _pd]),
     "fame_plan_destroy": (_i, [_vp]),
     "fame_set_stream": (_i, [_vp, _vp]),

@@ -282,6 +282,7 @@ def run_fame(args):
         dist.barrier()
     torch.cuda.synchronize()
     launches0 = lib.fame_kernel_launches()
+    host0 = lib.fame_host_launches()
     clocks.start()
     e0.record(stream)
     results, result_batches = [], []
@@ -293,6 +294,7 @@ def run_fame(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     launches = lib.fame_kernel_launches() - launches0
+    host_launches = lib.fame_host_launches() - host0
     if world > 1:
         dist.barrier()
     t = e0.elapsed_time(e1) / 1000.0
@@ -447,7 +449,9 @@ def run_fame(args):
                     "h2d_bytes_per_step": int(h2d / max(1, e2e_steps)),
                     "d2h_bytes_per_step": int(d2h / max(1, e2e_steps)), "steps": e2e_steps,
                     "path": "fame_plan_create (host geometry/material) + fame_band_solve + results to host"},
-            "roofline": roofline, "gpu_launches": int(launches), "clocks": clk,
+            "roofline": roofline, "gpu_launches": int(launches),
+            "host_launch_calls": int(host_launches),  # direct kernel launches + CUDA graph launches
+            "clocks": clk,
             "max_residual": res_max, "res_ok": bool(res_max <= RES_TOL), "worst_pair": worst, "status": status,
             "refinement": refine_report,
             "lanczos_steps_mean": float(np.mean(steps)), "cg_iters_per_kpoint_mean": float(np.mean(cgits)),

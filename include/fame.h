@@ -50,9 +50,13 @@ enum fame_handle { FAME_PR = 0, FAME_QR = 1, FAME_PRS = 2, FAME_QRS = 3 };
 /* Library version string. */
 const char* fame_version(void);
 
-/* Kernels launched by this library since it was loaded (all plans); a
- * diagnostic for benchmarks, no reference counterpart. */
+/* Kernels run by this library since it was loaded (all plans), and the
+ * launch calls it made from the host for them (a kernel launched directly
+ * counts once in both; a CUDA graph launch counts once here and its kernels
+ * in fame_kernel_launches).  Diagnostics for benchmarks, no reference
+ * counterpart. */
 long long fame_kernel_launches(void);
+long long fame_host_launches(void);
 
 /*
  * Create a plan for `nk` k-points of one n^3 grid.
