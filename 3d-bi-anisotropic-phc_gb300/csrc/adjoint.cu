@@ -192,6 +192,7 @@ int set_field(Plan& P, const double* eps, const double* gam) {
   P.gam_host.assign(gam, gam + Nq);
   int rc = upload_field<double>(P, P.d64, abg);
   if (rc == FAME_OK) rc = upload_field<float>(P, P.d32, abg);
+  if (rc == FAME_OK) rc = upload_tables_ds(P);  // the double-single copies, fields included
   if (rc != FAME_OK) return rc;
   cudaError_t e = cudaSuccess;
   if (!P.d_eps_gam) e = cudaMalloc(&P.d_eps_gam, sizeof(double) * 2 * (size_t)Nq);

@@ -70,7 +70,7 @@ static int autotune_prec(Plan& P, int nvec, int reps, TuneEntry* best_out) {
   };
   for (int div : {1, 2, 4, 8}) add((nvec + div - 1) / div);
   for (int c = 1; c <= 16; ++c) add(c);
-  const int prec = sizeof(R) == 4 ? FAME_C64 : FAME_C128;
+  const int prec = tune_prec<R>();
   const TuneEntry saved = tune_for(P, prec, nvec);
   cudaEvent_t ev[2];
   cudaEventCreate(&ev[0]);

@@ -311,6 +311,7 @@ int fame_plan_create(fame_plan_t* out, int n, int nk, const double* theta, const
   }
   rc = upload_tables<double>(P);
   if (rc == FAME_OK) rc = upload_tables<float>(P);
+  if (rc == FAME_OK) rc = upload_tables_ds(P);
   if (rc != FAME_OK) {
     g_static_error = P.last_error;
     fame_plan_destroy(h);
@@ -327,6 +328,7 @@ int fame_plan_destroy(fame_plan_t h) {
   else cudaDeviceSynchronize();
   free_tables(P.d64);
   free_tables(P.d32);
+  free_tables(P.dds);
   cudaFree(P.d_phase);
   cudaFree(P.d_work);
   cudaFree(P.d_inst);
@@ -367,6 +369,9 @@ int fame_set_option(fame_plan_t h, int option, double value) {
     case FAME_OPT_RELAX:
       if (!(value >= 0.0 && value < 1.0)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: relax must be in [0, 1)");
       P.opt_relax = value;
+      return FAME_OK;
+    case FAME_OPT_DS_RESIDUAL:
+      P.opt_ds_residual = value != 0.0;
       return FAME_OK;
     case FAME_OPT_RELAX_MAX:
       if (!(value >= 1.0 && value <= 1e8)) return fail(&P, FAME_ERR_BAD_ARG, "fame_set_option: relax_max must be in [1, 1e8]");
@@ -434,7 +439,10 @@ int run_op(fame_plan_t h, int prec, const void* x, void* y, int nvec, const int*
            long long out_len, const char* name, F&& body) {
   if (!h) return FAME_ERR_BAD_ARG;
   Plan& P = h->P;
-  if (prec != FAME_C128 && prec != FAME_C64) return fail(&P, FAME_ERR_BAD_ARG, std::string(name) + ": bad precision");
+  if (prec != FAME_C128 && prec != FAME_C64 && !(prec == FAME_C128_DS && std::string(name) == "fame_apply_B"))
+    return fail(&P, FAME_ERR_BAD_ARG, std::string(name) + ": bad precision");
+  if (prec == FAME_C128_DS && !ds_supported(P.n))
+    return fail(&P, FAME_ERR_UNSUPPORTED, std::string(name) + ": no double-single fncB for this grid size");
   if (nvec < 0 || (nvec > 0 && (!x || !y))) return fail(&P, FAME_ERR_BAD_ARG, std::string(name) + ": bad vectors");
   if (nvec == 0) return FAME_OK;
   if (inst)
@@ -494,6 +502,8 @@ int fame_apply_B(fame_plan_t h, int prec, const void* x, void* y, int nvec, cons
       float2* w0 = (float2*)P.d_work;
       float2* w1 = w0 + (size_t)nvec * 6 * P.Nq;
       e = launch_fncB<float>(P, (const float2*)xd, (float2*)yd, nvec, ctx, w0, w1, P.stream);
+    } else if (prec == FAME_C128_DS) {
+      e = launch_fncB_ds(P, (const double2*)xd, (double2*)yd, nvec, ctx, P.stream);
     } else {
       double2* w0 = (double2*)P.d_work;
       double2* w1 = w0 + (size_t)nvec * 6 * P.Nq;

@@ -113,6 +113,7 @@ struct Plan {
   // options (fame_set_option)
   int opt_precond = 1;                // CG on B preconditioned by the averaged-medium B0^{-1}
   double opt_tol32 = 1e-6;            // complex64 CG tolerance of the first refinement round
+  int opt_ds_residual = 1;            // mixed B^{-1}: residuals through the double-single fncB
   double opt_relax = 0.5;             // mixed Lanczos: relax the inner tolerance once Ritz residuals < this
   double opt_relax_max = 1e6;         // largest relaxation factor
   int opt_c64_round = 1;              // mixed B^{-1}: second round's B x update in complex64 (0: FP64 apply)
@@ -136,6 +137,7 @@ struct Plan {
   double* d_eps_gam = nullptr;        // field mode: [2][Nq] eps | gamma (FP64, gradient)
   PlanData<double> d64;
   PlanData<float> d32;
+  PlanData<ff> dds;  // double-single copies of the d64 tables (grids with ds_supported)
   // scratch: two 6-field work buffers per vector, sized for complex128
   void* d_work = nullptr;
   size_t work_vecs = 0;
@@ -164,6 +166,10 @@ struct Plan {
 
 // Tuned launch parameters for (prec, nvec), or the defaults.
 TuneEntry tune_for(const Plan& P, int prec, int nvec);
+// The tuning key of an arithmetic type (FAME_C64, FAME_C128, FAME_C128_DS).
+template <class R> constexpr int tune_prec() {
+  return std::is_same<R, float>::value ? FAME_C64 : std::is_same<R, double>::value ? FAME_C128 : FAME_C128_DS;
+}
 
 // Replay the launch sequence that `issue(stream)` enqueues, from a graph cached
 // under `key` (captured on first use on a private stream), on the plan's
@@ -196,6 +202,14 @@ cudaError_t launch_fncB(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const
                         cx<R>* w0, cx<R>* w1, cudaStream_t st, double2* pq = nullptr,
                         const cx<R>* pupd_z = nullptr, const double* pupd_beta = nullptr);
 template <class R> int fncB_pq_partials(const Plan& P, int nvec);
+// Grid sizes with a compiled double-single fncB (FAME_FOR_EACH_DS_N).
+bool ds_supported(int n);
+// y = B x for complex128 vectors, evaluated in double-single arithmetic
+// (x and y may alias; scratch: the plan's work arrays for nvec vectors).
+cudaError_t launch_fncB_ds(const Plan& P, const double2* x, double2* y, int nvec, const VecCtx& ctx,
+                           cudaStream_t st);
+// The plan's double-single tables, converted from its complex128 ones.
+int upload_tables_ds(Plan& P);
 template <class R>
 cudaError_t launch_fncA(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx,
                         cudaStream_t st);

@@ -91,11 +91,17 @@ __device__ __forceinline__ PiBlock<R> pi_load(const cx<R>* p) {
     P.p2[0] = mk<R>(b.z, b.w);
     P.p2[1] = mk<R>(c.x, c.y);
     P.p2[2] = mk<R>(c.z, c.w);
-  } else {
+  } else if constexpr (std::is_same<R, double>::value) {
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       P.p1[i] = __ldg(p + i);
       P.p2[i] = __ldg(p + 3 + i);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      P.p1[i] = p[i];
+      P.p2[i] = p[3 + i];
     }
   }
   P.sig = R(0);
@@ -634,20 +640,26 @@ inline dim3 grid_pts(long long Nq, int nvec, int tpb) {
 // Lanes per pencil of the split plane kernels for a tuned value (< 0: the
 // default of size N; 0: one thread per pencil) under the plan's option;
 // a count not compiled for N falls back to the default.
-template <int N> inline int plane_lanes(const Plan& P, int tuned) {
+template <class R, int N> inline int plane_lanes(const Plan& P, int tuned) {
+  if (std::is_same<R, ff>::value) return plane_split(N);  // double-single: the default split only
   if (!P.opt_plane_split || plane_split(N) == 0 || tuned == 0) return 0;
   for (int i = 0; i < kPlaneLanesMax; ++i)
     if (tuned > 0 && plane_lanes_alt(N, i) == tuned) return tuned;
   return plane_split(N);
 }
 
-// f(integral_constant<G>) for the compiled lane count G == lanes of size N.
-template <int N, class F> inline void with_lanes(int lanes, F&& f) {
-  static_for<0, kPlaneLanesMax>([&](auto ic) {
-    constexpr int G = plane_lanes_alt(N, decltype(ic)::value);
-    if constexpr (G > 0)
-      if (lanes == G) f(std::integral_constant<int, G>{});
-  });
+// f(integral_constant<G>) for the compiled lane count G == lanes of size N
+// (double-single: the default count only).
+template <class R, int N, class F> inline void with_lanes(int lanes, F&& f) {
+  static_assert(kPlaneLanesMax == 3, "one branch per compiled lane count");
+  constexpr bool ds = std::is_same<R, ff>::value;
+  constexpr int g0 = plane_lanes_alt(N, 0), g1 = ds ? 0 : plane_lanes_alt(N, 1), g2 = ds ? 0 : plane_lanes_alt(N, 2);
+  if constexpr (g0 > 0)
+    if (lanes == g0) return f(std::integral_constant<int, g0>{});
+  if constexpr (g1 > 0)
+    if (lanes == g1) return f(std::integral_constant<int, g1>{});
+  if constexpr (g2 > 0)
+    if (lanes == g2) return f(std::integral_constant<int, g2>{});
 }
 
 template <class R, int N, bool PREP, bool WITH_S>
@@ -657,10 +669,10 @@ cudaError_t plane_inv(const Plan& P, const PlanData<R>& d, const cx<R>* x, cx<R>
                       int tuned_lanes = -1) {
   const size_t sm = sizeof(cx<R>) * 3 * N * (N + 1);
   if constexpr (PREP && !WITH_S && plane_split(N) > 0) {
-    const int lanes = plane_lanes<N>(P, tuned_lanes);
+    const int lanes = plane_lanes<R, N>(P, tuned_lanes);
     if (lanes > 0) {
       cudaError_t e = cudaErrorInvalidValue;
-      with_lanes<N>(lanes, [&](auto gc) {
+      with_lanes<R, N>(lanes, [&](auto gc) {
         constexpr int G = decltype(gc)::value;
         auto kfn = k_plane_inv2<R, N, G>;
         e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -673,14 +685,18 @@ cudaError_t plane_inv(const Plan& P, const PlanData<R>& d, const cx<R>* x, cx<R>
       return e;
     }
   }
-  const int threads = ((3 * N + 31) / 32) * 32;
-  auto kfn = k_plane_inv<R, N, PREP, WITH_S>;
-  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return e;
-  FAME_LAUNCHED(1);
-  kfn<<<dim3(N, nside, nvec), threads, sm, st>>>(x, out, d, ctx, in_stride, in_side_stride, out_stride,
-                                                 side0, upd);
-  return cudaGetLastError();
+  if constexpr (std::is_same<R, ff>::value && PREP && !WITH_S && plane_split(N) > 0) {
+    return cudaErrorInvalidValue;  // double-single: split kernels only (above)
+  } else {
+    const int threads = ((3 * N + 31) / 32) * 32;
+    auto kfn = k_plane_inv<R, N, PREP, WITH_S>;
+    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    FAME_LAUNCHED(1);
+    kfn<<<dim3(N, nside, nvec), threads, sm, st>>>(x, out, d, ctx, in_stride, in_side_stride, out_stride,
+                                                   side0, upd);
+    return cudaGetLastError();
+  }
 }
 
 template <class R, int N, bool POST, bool WITH_S>
@@ -689,10 +705,10 @@ cudaError_t plane_fwd(const Plan& P, const PlanData<R>& d, const cx<R>* w, cx<R>
                       const VecCtx& ctx, cudaStream_t st, int tuned_lanes = -1) {
   const size_t sm = sizeof(cx<R>) * 3 * N * (N + 1);
   if constexpr (POST && !WITH_S && plane_split(N) > 0) {
-    const int lanes = plane_lanes<N>(P, tuned_lanes);
+    const int lanes = plane_lanes<R, N>(P, tuned_lanes);
     if (lanes > 0) {
       cudaError_t e = cudaErrorInvalidValue;
-      with_lanes<N>(lanes, [&](auto gc) {
+      with_lanes<R, N>(lanes, [&](auto gc) {
         constexpr int G = decltype(gc)::value;
         auto kfn = k_plane_fwd2<R, N, G>;
         e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -705,14 +721,18 @@ cudaError_t plane_fwd(const Plan& P, const PlanData<R>& d, const cx<R>* w, cx<R>
       return e;
     }
   }
-  const int threads = ((3 * N + 31) / 32) * 32;
-  auto kfn = k_plane_fwd<R, N, POST, WITH_S>;
-  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return e;
-  FAME_LAUNCHED(1);
-  kfn<<<dim3(N, nside, nvec), threads, sm, st>>>(w, y, d, ctx, w_stride, out_stride, out_side_stride,
-                                                 side0);
-  return cudaGetLastError();
+  if constexpr (std::is_same<R, ff>::value && POST && !WITH_S && plane_split(N) > 0) {
+    return cudaErrorInvalidValue;  // double-single: split kernels only (above)
+  } else {
+    const int threads = ((3 * N + 31) / 32) * 32;
+    auto kfn = k_plane_fwd<R, N, POST, WITH_S>;
+    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    FAME_LAUNCHED(1);
+    kfn<<<dim3(N, nside, nvec), threads, sm, st>>>(w, y, d, ctx, w_stride, out_stride, out_side_stride,
+                                                   side0);
+    return cudaGetLastError();
+  }
 }
 
 template <class R, int N, int DIR, int SMODE>
@@ -743,7 +763,7 @@ cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecC
   PlanData<R> d = pdata<R>(P);
   if (!P.opt_pi_table) d.pi = nullptr;  // evaluate Pi in the plane kernels instead
   const long long Nq = P.Nq;
-  const TuneEntry tn = tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec);
+  const TuneEntry tn = tune_for(P, tune_prec<R>(), nvec);
   const int chunk = (tn.chunk > 0 && tn.chunk < nvec) ? tn.chunk : nvec;
   for (int v0 = 0; v0 < nvec; v0 += chunk) {
     const int nv = std::min(chunk, nvec - v0);
@@ -846,3 +866,12 @@ cudaError_t handle_n(const Plan& P, int which, const cx<R>* x, cx<R>* y, int nve
                                                 cx<R>*, cudaStream_t);
 // explicit instantiation of one (precision, size)
 #define FAME_INST_SIZE(R, NN) FAME_SIZE_SIGS(template, R, NN)
+
+// Grid sizes with a compiled double-single fncB (the residuals b - B x of the
+// mixed inner solves; other sizes take the FP64 fncB), and its declaration.
+#define FAME_FOR_EACH_DS_N(X) X(12) X(60)
+#define FAME_DS_SIGS(PFX, NN)                                                                                      \
+  PFX cudaError_t fame::detail::fncB_n<fame::ff, NN>(const Plan&, const cx<fame::ff>*, cx<fame::ff>*, int,         \
+                                                     const VecCtx&, cx<fame::ff>*, cx<fame::ff>*, cudaStream_t,    \
+                                                     double2*, const cx<fame::ff>*, const double*);
+#define FAME_INST_DS(NN) FAME_DS_SIGS(template, NN)

@@ -21,6 +21,7 @@ namespace detail {
 template <class R> inline const PlanData<R>& pdata(const Plan& P);
 template <> inline const PlanData<double>& pdata<double>(const Plan& P) { return P.d64; }
 template <> inline const PlanData<float>& pdata<float>(const Plan& P) { return P.d32; }
+template <> inline const PlanData<ff>& pdata<ff>(const Plan& P) { return P.dds; }
 
 template <class R, int N>
 __global__ void __launch_bounds__(512)

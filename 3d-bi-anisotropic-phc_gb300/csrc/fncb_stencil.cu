@@ -74,8 +74,10 @@ inline dim3 grid_pts1(long long Nq, int nvec, int tpb) {
 
 // the size-templated transforms are instantiated elsewhere
 #define FAME_EXTERN(NN) FAME_SIZE_SIGS(extern template, float, NN) FAME_SIZE_SIGS(extern template, double, NN)
+#define FAME_EXTERN_DS(NN) FAME_DS_SIGS(extern template, NN)
 }  // namespace fame
 FAME_FOR_EACH_N(FAME_EXTERN)
+FAME_FOR_EACH_DS_N(FAME_EXTERN_DS)
 namespace fame {
 namespace detail {
 
@@ -113,11 +115,124 @@ cudaError_t build_pi_table(Plan& P) {
 template cudaError_t build_pi_table<float>(Plan&);
 template cudaError_t build_pi_table<double>(Plan&);
 
+// ---------------------------------------------------------------------------
+// Double-single fncB: complex128 in and out, complex float-float inside.
+// ---------------------------------------------------------------------------
+namespace {
+// out[i] = in[i] split into hi + lo (in place allowed: same 16-byte element);
+// with `active`, vector blockIdx.y of length len is skipped when inactive.
+__global__ void k_to_ds(const double2* in, cff* out, long long len, const int* active) {
+  if (active && !active[blockIdx.y]) return;
+  const long long o = (long long)blockIdx.y * len;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    const double2 v = in[o + i];
+    cff c;
+    c.x = ff(v.x);
+    c.y = ff(v.y);
+    out[o + i] = c;
+  }
+}
+__global__ void k_from_ds(const cff* in, double2* out, long long len, const int* active) {
+  if (active && !active[blockIdx.y]) return;
+  const long long o = (long long)blockIdx.y * len;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    const cff v = in[o + i];
+    out[o + i] = make_double2(double(v.x), double(v.y));
+  }
+}
+__global__ void k_real_to_ds(const double* in, ff* out, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = ff(in[i]);
+}
+inline unsigned conv_grid(long long n) {
+  const long long g = (n + 255) / 256;
+  return (unsigned)(g < 4096 ? (g > 0 ? g : 1) : 4096);
+}
+// dst = double-single copy of the n complex128 values at src (allocated on
+// first use)
+cudaError_t copy_to_ds(const double2* src, cff** dst, long long n, cudaStream_t st) {
+  if (!src) return cudaSuccess;
+  if (!*dst) {
+    cudaError_t e = cudaMalloc(dst, sizeof(cff) * (size_t)n);
+    if (e != cudaSuccess) {
+      *dst = nullptr;
+      return e;
+    }
+  }
+  FAME_LAUNCHED(1);
+  k_to_ds<<<dim3(conv_grid(n), 1), 256, 0, st>>>(src, *dst, n, nullptr);
+  return cudaGetLastError();
+}
+}  // namespace
+
+bool ds_supported(int n) {
+  switch (n) {
+#define FAME_CASE(NN) case NN: return true;
+    FAME_FOR_EACH_DS_N(FAME_CASE)
+#undef FAME_CASE
+    default: return false;
+  }
+}
+
+// (Re)builds the double-single tables from the complex128 ones; called at
+// plan creation and again when a field-mode plan's fields change.
+int upload_tables_ds(Plan& P) {
+  if (!ds_supported(P.n)) return FAME_OK;
+  const PlanData<double>& s = P.d64;
+  PlanData<ff>& d = P.dds;
+  cudaStream_t st = P.stream;
+  cudaError_t e = copy_to_ds(s.lam, &d.lam, (long long)P.nk * 3 * P.n, st);
+  if (e == cudaSuccess) e = copy_to_ds(s.tau, &d.tau, (long long)P.nk * 3, st);
+  if (e == cudaSuccess) e = copy_to_ds(s.sxyz, &d.sxyz, (long long)P.nk * 3 * P.n, st);
+  if (e == cudaSuccess) e = copy_to_ds(s.mat, &d.mat, (long long)P.nk * P.nphase * 27, st);
+  if (e == cudaSuccess) e = copy_to_ds(s.pi, &d.pi, (long long)P.nk * 6 * P.Nq, st);
+  if (e == cudaSuccess && s.fld) {
+    if (!d.fld) e = cudaMalloc(&d.fld, sizeof(ff) * 3 * (size_t)P.Nq);
+    if (e == cudaSuccess) {
+      FAME_LAUNCHED(1);
+      k_real_to_ds<<<conv_grid(3 * P.Nq), 256, 0, st>>>(s.fld, d.fld, 3 * P.Nq);
+      e = cudaGetLastError();
+    }
+  }
+  for (int i = 0; i < 9; ++i) d.gram[i] = ff(s.gram[i]);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? FAME_OK : cuda_fail(&P, e, "double-single tables");
+}
+
+cudaError_t launch_fncB_ds(const Plan& P, const double2* x, double2* y, int nvec, const VecCtx& ctx,
+                           cudaStream_t st) {
+  if (nvec <= 0) return cudaSuccess;
+  const long long len = 4 * P.Nq;  // one vector
+  const unsigned gx = std::min(conv_grid(len), 256u);
+  cff* yd = reinterpret_cast<cff*>(y);
+  FAME_LAUNCHED(1);
+  k_to_ds<<<dim3(gx, nvec), 256, 0, st>>>(x, yd, len, ctx.active);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  cff* w0 = reinterpret_cast<cff*>(P.d_work);
+  cff* w1 = w0 + (size_t)nvec * 6 * P.Nq;
+  // x and y of the transforms alias: every sub-batch reads its vectors in its
+  // first kernel and writes them in its last
+  switch (P.n) {
+#define FAME_CASE(NN)                                                                            \
+  case NN:                                                                                       \
+    e = fncB_n<ff, NN>(P, yd, yd, nvec, ctx, w0, w1, st, nullptr, nullptr, nullptr);             \
+    break;
+    FAME_FOR_EACH_DS_N(FAME_CASE)
+#undef FAME_CASE
+    default: return cudaErrorInvalidValue;
+  }
+  if (e != cudaSuccess) return e;
+  FAME_LAUNCHED(1);
+  k_from_ds<<<dim3(gx, nvec), 256, 0, st>>>(yd, y, len, ctx.active);
+  return cudaGetLastError();
+}
+
 // Partials per vector that fncB's pq output receives for a batch of nvec, or
 // 0 when the tuned form of that batch does not produce them.
 template <class R>
 int fncB_pq_partials(const Plan& P, int nvec) {
-  if (tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).stencil_tpb != 0) return 0;
+  if (tune_for(P, tune_prec<R>(), nvec).stencil_tpb != 0) return 0;
   switch (P.n) {
 #define FAME_CASE(NN) case NN: return sweep_partials_n<R, NN>();
     FAME_FOR_EACH_N(FAME_CASE)

@@ -206,8 +206,8 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
                                        (uintptr_t)w0, (uintptr_t)w1, (uintptr_t)s, (uintptr_t)part, (uintptr_t)part2,
                                        (uintptr_t)d_inst, (uintptr_t)nblk, (uintptr_t)nblkv,
                                        sizeof(R) == 4 ? (uintptr_t)P.d32.pc : (uintptr_t)P.d64.pc,
-                                       (uintptr_t)tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).chunk,
-                                       (uintptr_t)tune_for(P, sizeof(R) == 4 ? FAME_C64 : FAME_C128, nvec).stencil_tpb,
+                                       (uintptr_t)tune_for(P, tune_prec<R>(), nvec).chunk,
+                                       (uintptr_t)tune_for(P, tune_prec<R>(), nvec).stencil_tpb,
                                        (uintptr_t)nblk_pq, (uintptr_t)P.opt_plane_split,
                                        (uintptr_t)P.opt_pi_table};
   bool use_graph = P.opt_graph != 0;
@@ -379,10 +379,15 @@ int solve_B_mixed(Plan& P, const double2* b, double2* x, double2* Bx, int nvec, 
       }
     FAME_CK(refine_acc(x, d32, L, nvec, dmask, st, dscale + nvec), "mixed acc");
     if (round != 1 || !P.opt_c64_round) {
-      // exact FP64 residual b - B x
-      double2* w0 = (double2*)P.d_work;
-      double2* w1 = w0 + (size_t)nvec * 6 * P.Nq;
-      FAME_CK(launch_fncB<double>(P, x, Bx, nvec, ctx, w0, w1, st), "mixed fncB");
+      // exact residual b - B x: fncB in double-single arithmetic where the
+      // grid has it (~1e-14 relative, on the FP32 pipes), else FP64
+      if (P.opt_ds_residual && ds_supported(P.n)) {
+        FAME_CK(launch_fncB_ds(P, x, Bx, nvec, ctx, st), "mixed fncB");
+      } else {
+        double2* w0 = (double2*)P.d_work;
+        double2* w1 = w0 + (size_t)nvec * 6 * P.Nq;
+        FAME_CK(launch_fncB<double>(P, x, Bx, nvec, ctx, w0, w1, st), "mixed fncB");
+      }
       for (int v = 0; v < nvec; ++v) {
         if (b64_applies) *b64_applies += m[v];
         if (b64_vec) b64_vec[v] += m[v];

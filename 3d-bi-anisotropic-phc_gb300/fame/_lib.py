@@ -23,6 +23,7 @@ FAME_ERR_SINGULAR = 7
 FAME_ERR_ALLOC = 8
 FAME_C128 = 0
 FAME_C64 = 1
+FAME_C128_DS = 2
 FAME_PR, FAME_QR, FAME_PRS, FAME_QRS = 0, 1, 2, 3
 FAME_HOST_PTR = 1
 FAME_OPT_PRECOND = 0
@@ -37,6 +38,7 @@ FAME_OPT_PI_TABLE = 8
 FAME_OPT_C64_ROUND = 9
 FAME_OPT_RELAX = 10
 FAME_OPT_RELAX_MAX = 11
+FAME_OPT_DS_RESIDUAL = 12
 FAME_SHAPE_WOODPILE, FAME_SHAPE_SPHERE, FAME_SHAPE_TETRA = 0, 1, 2
 FAME_RASTER_PAINT = 2
 

@@ -209,13 +209,14 @@ class Plan:
     def set_option(self, option, value):
         """fame_set_option: 'precond' (bool), 'tol32' (float), 'graph' (0, 1 or 2), 'itol_floor' (float),
         'plane_split' (bool), 'sira_nearest' (bool), 'refine' (bool), 'refine_tol' (float),
-        'pi_table' (bool), 'c64_round' (bool), 'relax' (float in [0, 1)) or 'relax_max' (float >= 1)."""
+        'pi_table' (bool), 'c64_round' (bool), 'relax' (float in [0, 1)), 'relax_max' (float >= 1) or
+        'ds_residual' (bool)."""
         code = {"precond": L.FAME_OPT_PRECOND, "tol32": L.FAME_OPT_TOL32, "graph": L.FAME_OPT_GRAPH,
                 "itol_floor": L.FAME_OPT_ITOL_FLOOR, "plane_split": L.FAME_OPT_PLANE_SPLIT,
                 "sira_nearest": L.FAME_OPT_SIRA_NEAREST, "refine": L.FAME_OPT_REFINE,
                 "refine_tol": L.FAME_OPT_REFINE_TOL, "pi_table": L.FAME_OPT_PI_TABLE,
                 "c64_round": L.FAME_OPT_C64_ROUND, "relax": L.FAME_OPT_RELAX,
-                "relax_max": L.FAME_OPT_RELAX_MAX}.get(option, option)
+                "relax_max": L.FAME_OPT_RELAX_MAX, "ds_residual": L.FAME_OPT_DS_RESIDUAL}.get(option, option)
         check(self._lib.fame_set_option(self._h, int(code), float(value)), self._h, "fame_set_option")
         return self
 

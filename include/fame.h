@@ -41,7 +41,10 @@ enum fame_status {
   FAME_ERR_ALLOC = 8
 };
 
-enum fame_precision { FAME_C128 = 0, FAME_C64 = 1 };
+/* FAME_C128_DS: complex128 vectors, the operator evaluated in double-single
+ * (float-float) arithmetic, ~1e-14 relative (fame_apply_B only; grids with a
+ * compiled double-single fncB, else FAME_ERR_UNSUPPORTED). */
+enum fame_precision { FAME_C128 = 0, FAME_C64 = 1, FAME_C128_DS = 2 };
 
 enum fame_handle { FAME_PR = 0, FAME_QR = 1, FAME_PRS = 2, FAME_QRS = 3 };
 
@@ -127,13 +130,19 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *                     wanted pairs with a weight of about r).  The
  *                     Gamma-like instances at the tolerance floor are not
  *                     relaxed.
+ *   FAME_OPT_DS_RESIDUAL  mixed B^{-1}: the refinement rounds' residuals
+ *                     b - B x take fncB in double-single arithmetic instead
+ *                     of FP64 where the grid has it compiled [1] (FP32 pipes
+ *                     instead of GB300's FP64 pipe; ~1e-14 relative).  The
+ *                     reported NFSEP residuals and the refinement sweep keep
+ *                     FP64.
  *   FAME_OPT_RELAX_MAX  the largest factor of that relaxation [1e6].  The error
  *                     such a solve adds to a wanted pair is bounded by about
  *                     (inner tolerance) x c whatever the factor. */
 enum fame_option {
   FAME_OPT_PRECOND = 0, FAME_OPT_TOL32 = 1, FAME_OPT_GRAPH = 2, FAME_OPT_ITOL_FLOOR = 3, FAME_OPT_PLANE_SPLIT = 4,
   FAME_OPT_SIRA_NEAREST = 5, FAME_OPT_REFINE = 6, FAME_OPT_REFINE_TOL = 7, FAME_OPT_PI_TABLE = 8,
-  FAME_OPT_C64_ROUND = 9, FAME_OPT_RELAX = 10, FAME_OPT_RELAX_MAX = 11
+  FAME_OPT_C64_ROUND = 9, FAME_OPT_RELAX = 10, FAME_OPT_RELAX_MAX = 11, FAME_OPT_DS_RESIDUAL = 12
 };
 int fame_set_option(fame_plan_t plan, int option, double value);
 
