@@ -46,20 +46,30 @@ static void put_tune(Plan& P, const TuneEntry& t) {
 
 template <class R>
 static int autotune_prec(Plan& P, int nvec, int reps, TuneEntry* best_out) {
+  // the double-single operator takes complex128 vectors
+  constexpr bool ds = std::is_same<R, ff>::value;
+  using IO = typename std::conditional<ds, double, R>::type;
   cudaStream_t st = P.stream;
   const long long L = 4 * P.Nq;
   cudaError_t e;
-  cx<R>* x = (cx<R>*)workspace(P, 60, sizeof(cx<R>) * L * nvec, &e);
+  cx<IO>* x = (cx<IO>*)workspace(P, 60, sizeof(cx<IO>) * L * nvec, &e);
   if (e != cudaSuccess) return cuda_fail(&P, e, "autotune buffers");
-  cx<R>* y = (cx<R>*)workspace(P, 61, sizeof(cx<R>) * L * nvec, &e);
+  cx<IO>* y = (cx<IO>*)workspace(P, 61, sizeof(cx<IO>) * L * nvec, &e);
   if (e != cudaSuccess) return cuda_fail(&P, e, "autotune buffers");
-  e = cudaMemsetAsync(x, 0x3c, sizeof(cx<R>) * L * nvec, st);  // finite, normal values
+  e = cudaMemsetAsync(x, 0x3c, sizeof(cx<IO>) * L * nvec, st);  // finite, normal values
   if (e == cudaSuccess) e = ensure_work(P, nvec);
   if (e != cudaSuccess) return cuda_fail(&P, e, "autotune setup");
-  cx<R>* w0 = (cx<R>*)P.d_work;
-  cx<R>* w1 = w0 + (size_t)nvec * 6 * P.Nq;
   VecCtx ctx;
   ctx.nk = P.nk;
+  auto launch = [&]() -> cudaError_t {
+    if constexpr (ds) {
+      return launch_fncB_ds(P, x, y, nvec, ctx, st);
+    } else {
+      cx<R>* w0 = (cx<R>*)P.d_work;
+      cx<R>* w1 = w0 + (size_t)nvec * 6 * P.Nq;
+      return launch_fncB<R>(P, x, y, nvec, ctx, w0, w1, st);
+    }
+  };
   // The whole batch, halves, quarters and eighths, and every width up to 16:
   // the plane kernels launch 2n CTAs per vector, and how well a width fills
   // the last wave of resident CTAs (2 per SM at n = 60) matters as much as
@@ -80,11 +90,11 @@ static int autotune_prec(Plan& P, int nvec, int reps, TuneEntry* best_out) {
   // median time of one fncB on the batch with t installed (microseconds)
   auto time_one = [&](TuneEntry& t) -> cudaError_t {
     put_tune(P, t);
-    cudaError_t e2 = launch_fncB<R>(P, x, y, nvec, ctx, w0, w1, st);  // warm-up
+    cudaError_t e2 = launch();  // warm-up
     std::vector<float> ms;
     for (int r = 0; r < reps && e2 == cudaSuccess; ++r) {
       cudaEventRecord(ev[0], st);
-      e2 = launch_fncB<R>(P, x, y, nvec, ctx, w0, w1, st);
+      e2 = launch();
       cudaEventRecord(ev[1], st);
       if (e2 == cudaSuccess) e2 = cudaEventSynchronize(ev[1]);
       float m = 0.f;
@@ -110,7 +120,8 @@ static int autotune_prec(Plan& P, int nvec, int reps, TuneEntry* best_out) {
     }
   // the plane kernels' split, with the best chunk and stencil form
   if (e == cudaSuccess && P.opt_plane_split && plane_split(P.n) > 0) {
-    std::vector<int> lanes = {0};
+    std::vector<int> lanes;
+    if (!ds) lanes.push_back(0);  // one thread per pencil (not compiled in double-single)
     for (int i = 1; i < kPlaneLanesMax; ++i)
       if (plane_lanes_alt(P.n, i) > 0) lanes.push_back(plane_lanes_alt(P.n, i));
     const TuneEntry base = best;
@@ -142,9 +153,14 @@ extern "C" {
 int fame_autotune(fame_plan_t h, int prec, int nvec, int* chunk, int* stencil_tpb, double* us) {
   if (!h) return FAME_ERR_BAD_ARG;
   Plan& P = h->P;
-  if (nvec < 1 || (prec != FAME_C64 && prec != FAME_C128)) return fail(&P, FAME_ERR_BAD_ARG, "fame_autotune: bad argument");
+  if (nvec < 1 || (prec != FAME_C64 && prec != FAME_C128 && prec != FAME_C128_DS))
+    return fail(&P, FAME_ERR_BAD_ARG, "fame_autotune: bad argument");
+  if (prec == FAME_C128_DS && !ds_supported(P.n))
+    return fail(&P, FAME_ERR_UNSUPPORTED, "fame_autotune: no double-single fncB for this grid size");
   TuneEntry b;
-  const int rc = prec == FAME_C64 ? autotune_prec<float>(P, nvec, 5, &b) : autotune_prec<double>(P, nvec, 5, &b);
+  const int rc = prec == FAME_C64    ? autotune_prec<float>(P, nvec, 5, &b)
+                 : prec == FAME_C128 ? autotune_prec<double>(P, nvec, 5, &b)
+                                     : autotune_prec<ff>(P, nvec, 5, &b);
   if (rc != FAME_OK) return rc;
   if (chunk) *chunk = b.chunk;
   if (stencil_tpb) *stencil_tpb = b.stencil_tpb;
@@ -156,7 +172,7 @@ int fame_set_tune(fame_plan_t h, int prec, int nvec, int chunk, int stencil_tpb)
   if (!h) return FAME_ERR_BAD_ARG;
   Plan& P = h->P;
   if (nvec < 1 || chunk < 0 || (stencil_tpb != 0 && stencil_tpb != 128 && stencil_tpb != 256 && stencil_tpb != 512) ||
-      (prec != FAME_C64 && prec != FAME_C128))
+      (prec != FAME_C64 && prec != FAME_C128 && prec != FAME_C128_DS))
     return fail(&P, FAME_ERR_BAD_ARG, "fame_set_tune: bad argument");
   TuneEntry t = tune_for(P, prec, nvec);  // keeps the width's split
   t.chunk = chunk >= nvec ? 0 : chunk;
@@ -168,7 +184,7 @@ int fame_set_tune(fame_plan_t h, int prec, int nvec, int chunk, int stencil_tpb)
 int fame_set_tune_lanes(fame_plan_t h, int prec, int nvec, int lanes) {
   if (!h) return FAME_ERR_BAD_ARG;
   Plan& P = h->P;
-  if (nvec < 1 || lanes < -1 || lanes > 64 || (prec != FAME_C64 && prec != FAME_C128))
+  if (nvec < 1 || lanes < -1 || lanes > 64 || (prec != FAME_C64 && prec != FAME_C128 && prec != FAME_C128_DS))
     return fail(&P, FAME_ERR_BAD_ARG, "fame_set_tune_lanes: bad argument");
   TuneEntry t = tune_for(P, prec, nvec);
   t.lanes = lanes;
@@ -179,7 +195,8 @@ int fame_set_tune_lanes(fame_plan_t h, int prec, int nvec, int lanes) {
 int fame_get_tune(fame_plan_t h, int prec, int nvec, int* chunk, int* stencil_tpb, int* lanes) {
   if (!h) return FAME_ERR_BAD_ARG;
   Plan& P = h->P;
-  if (nvec < 1 || (prec != FAME_C64 && prec != FAME_C128)) return fail(&P, FAME_ERR_BAD_ARG, "fame_get_tune: bad argument");
+  if (nvec < 1 || (prec != FAME_C64 && prec != FAME_C128 && prec != FAME_C128_DS))
+    return fail(&P, FAME_ERR_BAD_ARG, "fame_get_tune: bad argument");
   const TuneEntry t = tune_for(P, prec, nvec);
   if (chunk) *chunk = t.chunk;
   if (stencil_tpb) *stencil_tpb = t.stencil_tpb;

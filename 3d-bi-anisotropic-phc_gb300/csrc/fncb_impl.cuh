@@ -121,6 +121,29 @@ template <class R> __device__ __forceinline__ R rsqrt_n3(int n) {
   return R(1) / sqrt(R(n) * R(n) * R(n));
 }
 
+// Operator input / output of the split plane kernels.  The double-single
+// operator reads and writes complex128 vectors (the caller's), converting
+// on load and store, so it needs no conversion passes; the conversions run
+// on the FP64 pipe, which its float-float arithmetic leaves idle.
+template <class R> __device__ __forceinline__ cx<R> load_io(const cx<R>* p) {
+  if constexpr (std::is_same<R, ff>::value) {
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    cff c;
+    c.x = ff(v.x);
+    c.y = ff(v.y);
+    return c;
+  } else {
+    return *p;
+  }
+}
+template <class R> __device__ __forceinline__ void store_io(cx<R>* p, cx<R> v) {
+  if constexpr (std::is_same<R, ff>::value) {
+    *reinterpret_cast<double2*>(p) = make_double2(double(v.x), double(v.y));
+  } else {
+    *p = v;
+  }
+}
+
 // The conjugate-gradient direction update p = z + beta p, done by the first
 // kernel of fncB on the p it reads (z == null: no update).  Each CTA rewrites
 // the plane of p it loads, so the separate update pass over p disappears.
@@ -433,8 +456,8 @@ k_plane_inv2(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d
     for (int it = 0; it < ITEMS; ++it) {
       const int e = tid + it * T;
       if (tid < T && e < N * N) {
-        in[it][0] = xin[e];
-        in[it][1] = xin[Nq + e];
+        in[it][0] = load_io<R>(xin + e);
+        in[it][1] = load_io<R>(xin + Nq + e);
       }
     }
     if (upd.z) {  // p = z + beta p, written back
@@ -596,8 +619,8 @@ k_plane_fwd2(const cx<R>* __restrict__ w, cx<R>* __restrict__ y, PlanData<R> d, 
       a = cfmac(P.p1[2], u2, cfmac(P.p1[1], u1, cmulc(P.p1[0], u0)));
       b = cfmac(P.p2[2], u2, cfmac(P.p2[1], u1, cmulc(P.p2[0], u0)));
     }
-    o[e] = cscale(a, sc);
-    o[Nq + e] = cscale(b, sc);
+    store_io<R>(o + e, cscale(a, sc));
+    store_io<R>(o + Nq + e, cscale(b, sc));
   }
 }
 
@@ -641,19 +664,17 @@ inline dim3 grid_pts(long long Nq, int nvec, int tpb) {
 // default of size N; 0: one thread per pencil) under the plan's option;
 // a count not compiled for N falls back to the default.
 template <class R, int N> inline int plane_lanes(const Plan& P, int tuned) {
-  if (std::is_same<R, ff>::value) return plane_split(N);  // double-single: the default split only
-  if (!P.opt_plane_split || plane_split(N) == 0 || tuned == 0) return 0;
+  if (std::is_same<R, ff>::value && (tuned == 0 || !P.opt_plane_split)) tuned = -1;  // double-single: split only
+  else if (!P.opt_plane_split || plane_split(N) == 0 || tuned == 0) return 0;
   for (int i = 0; i < kPlaneLanesMax; ++i)
     if (tuned > 0 && plane_lanes_alt(N, i) == tuned) return tuned;
   return plane_split(N);
 }
 
-// f(integral_constant<G>) for the compiled lane count G == lanes of size N
-// (double-single: the default count only).
+// f(integral_constant<G>) for the compiled lane count G == lanes of size N.
 template <class R, int N, class F> inline void with_lanes(int lanes, F&& f) {
   static_assert(kPlaneLanesMax == 3, "one branch per compiled lane count");
-  constexpr bool ds = std::is_same<R, ff>::value;
-  constexpr int g0 = plane_lanes_alt(N, 0), g1 = ds ? 0 : plane_lanes_alt(N, 1), g2 = ds ? 0 : plane_lanes_alt(N, 2);
+  constexpr int g0 = plane_lanes_alt(N, 0), g1 = plane_lanes_alt(N, 1), g2 = plane_lanes_alt(N, 2);
   if constexpr (g0 > 0)
     if (lanes == g0) return f(std::integral_constant<int, g0>{});
   if constexpr (g1 > 0)
@@ -735,13 +756,68 @@ cudaError_t plane_fwd(const Plan& P, const PlanData<R>& d, const cx<R>* w, cx<R>
   }
 }
 
+// ---------------------------------------------------------------------------
+// col2: the z-DFT with the same prime-factor split as the plane kernels, for
+// the double-single type (one thread holding a whole 60-point column of
+// float-float pairs needs 240 registers of data alone).  One CTA per
+// (y row, field, vector): the row's N columns (all z) are staged in shared
+// memory with coalesced row loads, G threads per column do the length-G
+// passes in place, then each the length-M DFT of its sub-pencil in
+// registers, written straight back to global (consecutive threads hold
+// consecutive x).  Scale 1/sqrt(n), no S multiply.
+// ---------------------------------------------------------------------------
+template <class R, int N, int DIR>
+__global__ void __launch_bounds__(((N * plane_split(N) + 31) / 32) * 32)
+k_col2(cx<R>* __restrict__ w, VecCtx ctx, long long stride) {
+  constexpr int G = plane_split(N);
+  using SP = Split<N, G>;
+  constexpr int M = SP::M, LD = N + 1, T = N * G;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);  // [z][LD]
+  const int y = blockIdx.x;
+  const int vec = blockIdx.z;
+  if (ctx.active && !ctx.active[vec]) return;
+  const long long NN = (long long)N * N;
+  cx<R>* base = w + vec * stride + (long long)blockIdx.y * N * NN + (long long)y * N;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < N * N; e += blockDim.x) {
+    const int z = e / N, x = e - z * N;
+    sm[z * LD + x] = base[(long long)z * NN + x];
+  }
+  __syncthreads();
+  const int g = tid / N, p = tid - g * N;
+  const bool act = tid < T;
+  if (act) with_g<G>(g, [&](auto gc) { split_pass_a<R, N, G, DIR, LD, decltype(gc)::value>(sm + p); });
+  __syncthreads();
+  if (act) {
+    cx<R> z[M];
+    with_g<G>(g, [&](auto gc) { split_pass_b_load<R, N, G, LD, decltype(gc)::value>(sm + p, z); });
+    fft<R, M, DIR>(z);
+    const R scale = R(1) / sqrt(R(N));
+#pragma unroll
+    for (int i = 0; i < M; ++i) z[i] = cscale(z[i], scale);
+    with_g<G>(g, [&](auto gc) { split_pass_b_store<R, N, G, (int)(N * N), decltype(gc)::value>(base + p, z); });
+  }
+}
+
 template <class R, int N, int DIR, int SMODE>
 cudaError_t col(const PlanData<R>& d, cx<R>* w, int nfield, int nvec, long long stride, const VecCtx& ctx,
                 cudaStream_t st) {
-  dim3 g((N * N + 127) / 128, nfield, nvec);
-  FAME_LAUNCHED(1);
-  k_col<R, N, DIR, SMODE><<<g, 128, 0, st>>>(w, d, ctx, stride);
-  return cudaGetLastError();
+  if constexpr (std::is_same<R, ff>::value && SMODE == 0 && plane_split(N) > 0) {
+    constexpr int G = plane_split(N);
+    const size_t sm = sizeof(cx<R>) * N * (N + 1);
+    auto kfn = k_col2<R, N, DIR>;
+    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    FAME_LAUNCHED(1);
+    kfn<<<dim3(N, nfield, nvec), ((N * G + 31) / 32) * 32, sm, st>>>(w, ctx, stride);
+    return cudaGetLastError();
+  } else {
+    dim3 g((N * N + 127) / 128, nfield, nvec);
+    FAME_LAUNCHED(1);
+    k_col<R, N, DIR, SMODE><<<g, 128, 0, st>>>(w, d, ctx, stride);
+    return cudaGetLastError();
+  }
 }
 
 

@@ -132,14 +132,6 @@ __global__ void k_to_ds(const double2* in, cff* out, long long len, const int* a
     out[o + i] = c;
   }
 }
-__global__ void k_from_ds(const cff* in, double2* out, long long len, const int* active) {
-  if (active && !active[blockIdx.y]) return;
-  const long long o = (long long)blockIdx.y * len;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
-    const cff v = in[o + i];
-    out[o + i] = make_double2(double(v.x), double(v.y));
-  }
-}
 __global__ void k_real_to_ds(const double* in, ff* out, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     out[i] = ff(in[i]);
@@ -202,30 +194,19 @@ int upload_tables_ds(Plan& P) {
 cudaError_t launch_fncB_ds(const Plan& P, const double2* x, double2* y, int nvec, const VecCtx& ctx,
                            cudaStream_t st) {
   if (nvec <= 0) return cudaSuccess;
-  const long long len = 4 * P.Nq;  // one vector
-  const unsigned gx = std::min(conv_grid(len), 256u);
+  // the first and last kernels of the double-single fncB read and write
+  // complex128 elements (load_io / store_io): the vectors are passed as they are
+  const cff* xd = reinterpret_cast<const cff*>(x);
   cff* yd = reinterpret_cast<cff*>(y);
-  FAME_LAUNCHED(1);
-  k_to_ds<<<dim3(gx, nvec), 256, 0, st>>>(x, yd, len, ctx.active);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
   cff* w0 = reinterpret_cast<cff*>(P.d_work);
   cff* w1 = w0 + (size_t)nvec * 6 * P.Nq;
-  // x and y of the transforms alias: every sub-batch reads its vectors in its
-  // first kernel and writes them in its last
   switch (P.n) {
-#define FAME_CASE(NN)                                                                            \
-  case NN:                                                                                       \
-    e = fncB_n<ff, NN>(P, yd, yd, nvec, ctx, w0, w1, st, nullptr, nullptr, nullptr);             \
-    break;
+#define FAME_CASE(NN) \
+  case NN: return fncB_n<ff, NN>(P, xd, yd, nvec, ctx, w0, w1, st, nullptr, nullptr, nullptr);
     FAME_FOR_EACH_DS_N(FAME_CASE)
 #undef FAME_CASE
     default: return cudaErrorInvalidValue;
   }
-  if (e != cudaSuccess) return e;
-  FAME_LAUNCHED(1);
-  k_from_ds<<<dim3(gx, nvec), 256, 0, st>>>(yd, y, len, ctx.active);
-  return cudaGetLastError();
 }
 
 // Partials per vector that fncB's pq output receives for a batch of nvec, or

@@ -36,6 +36,16 @@ def _prec_of(x):
     raise TypeError(f"unsupported dtype {x.dtype}")
 
 
+def _tune_prec(prec):
+    """Tuning key of 'c64', 'c128' or 'c128ds' (complex128 vectors, double-single
+    arithmetic: the mixed inner solves' residuals), or the FAME_* code itself."""
+    if prec in ("c64", L.FAME_C64):
+        return L.FAME_C64
+    if prec in ("c128ds", L.FAME_C128_DS):
+        return L.FAME_C128_DS
+    return L.FAME_C128
+
+
 class Plan:
     """``fame_plan_create`` wrapper (replaces the per-k mtx_A / mtx_B / fnc setup)."""
 
@@ -230,9 +240,9 @@ class Plan:
         import json
         import os
         nvec = self.nk if nvec is None else int(nvec)
-        pr = L.FAME_C64 if prec in ("c64", L.FAME_C64) else L.FAME_C128
+        pr = _tune_prec(prec)
         dev = torch.cuda.get_device_name() if torch is not None and torch.cuda.is_available() else "gpu"
-        key = f"{dev}|n={self.n}|{'c64' if pr == L.FAME_C64 else 'c128'}|nvec={nvec}"
+        key = f"{dev}|n={self.n}|{ {L.FAME_C64: 'c64', L.FAME_C128: 'c128'}.get(pr, 'c128ds') }|nvec={nvec}"
         table = {}
         if cache and os.path.exists(cache):
             with open(cache) as f:
@@ -259,14 +269,14 @@ class Plan:
         """fame_set_tune + fame_set_tune_lanes: install fncB launch parameters
         measured before (on another plan of the same grid, precision and
         batch width)."""
-        pr = L.FAME_C64 if prec in ("c64", L.FAME_C64) else L.FAME_C128
+        pr = _tune_prec(prec)
         check(self._lib.fame_set_tune(self._h, pr, int(nvec), int(chunk), int(stencil_tpb)), self._h,
               "fame_set_tune")
         check(self._lib.fame_set_tune_lanes(self._h, pr, int(nvec), int(lanes)), self._h, "fame_set_tune_lanes")
 
     def get_tune(self, prec, nvec):
         """fame_get_tune: the installed dict(chunk, stencil_tpb, lanes)."""
-        pr = L.FAME_C64 if prec in ("c64", L.FAME_C64) else L.FAME_C128
+        pr = _tune_prec(prec)
         ch, tpb, ln = C.c_int(), C.c_int(), C.c_int()
         check(self._lib.fame_get_tune(self._h, pr, int(nvec), C.byref(ch), C.byref(tpb), C.byref(ln)), self._h,
               "fame_get_tune")

@@ -223,12 +223,14 @@ def run_fame(args):
     plans = {b: fame.woodpile_plan(N_GRID, batches[b]) for b in needed}
     # fncB launch parameters timed once on one plan (fame_autotune) and
     # installed on every plan of the run (fame_set_tune)
-    # (complex64 for the inner CG, complex128 for the FP64 residual refinement)
+    # (complex64 for the inner CG, double-single for the inner solves' residuals,
+    # complex128 for the refinement sweep and the NFSEP checks)
     tune = plans[needed[0]].autotune(nvec=args.batch, prec="c64")
     tune128 = plans[needed[0]].autotune(nvec=args.batch, prec="c128")
+    tuneds = plans[needed[0]].autotune(nvec=args.batch, prec="c128ds")
 
     def set_tune(pl):
-        for pr, t in ((1, tune), (0, tune128)):
+        for pr, t in ((1, tune), (0, tune128), (2, tuneds)):
             pl.set_tune(pr, args.batch, int(t["chunk"]), int(t["stencil_tpb"]), int(t.get("lanes", -1)))
 
     for pl in plans.values():
@@ -439,8 +441,9 @@ def run_fame(args):
                            batching="consecutive path points, the two Gamma points in one batch",
                            fncb_tune={k: int(tune[k]) for k in ("chunk", "stencil_tpb", "lanes")},
                            fncb_tune_c128={k: int(tune128[k]) for k in ("chunk", "stencil_tpb", "lanes")},
-                           precision="complex64 fncB + preconditioned CG, FP64 recurrence/reorth/residual "
-                                     f"refinement (B^-1 to {INNER_TOL_MIXED:g}, tighter near Gamma, relaxed by "
+                           fncb_tune_c128ds={k: int(tuneds[k]) for k in ("chunk", "stencil_tpb", "lanes")},
+                           precision="complex64 fncB + preconditioned CG, FP64 recurrence/reorth, residual "
+                                     f"refinement with the double-single fncB (B^-1 to {INNER_TOL_MIXED:g}, tighter near Gamma, relaxed by "
                                      "0.5 / (largest relative Ritz residual) for later Lanczos vectors), FP64 "
                                      "Rayleigh-Ritz refinement sweep of every Ritz pair, FP64 NFSEP check",
                            l2="inputs larger than L2 (Lanczos basis and B*Q of a batch "
@@ -585,8 +588,18 @@ def profile_fncb(nvec, prec, tune=None):
         plan.set_tune(prec, nvec, tune[0], tune[1], tune[2] if len(tune) > 2 else -1)
     dt = torch.complex64 if prec == "c64" else torch.complex128
     x = torch.randn(nvec, 4 * N_GRID ** 3, dtype=dt, device="cuda")
-    for _ in range(3):
-        y = plan.apply_B(x)
+    if prec == "c128ds":  # complex128 vectors, double-single arithmetic (fame_apply_B, FAME_C128_DS)
+        import ctypes
+        lib = fame.load()
+        y = torch.empty_like(x)
+        lib.fame_set_stream(plan.raw, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        for _ in range(3):
+            rc = lib.fame_apply_B(plan.raw, 2, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()), nvec,
+                                  None, 0)
+            fame._lib.check(rc, plan.raw, "fame_apply_B")
+    else:
+        for _ in range(3):
+            y = plan.apply_B(x)
     torch.cuda.synchronize()
     print(f"fncB {prec} n={N_GRID} x{nvec}: ok, |y| = {float(torch.linalg.norm(y)):.6e}")
     plan.close()
@@ -641,7 +654,7 @@ def main():
     ap.add_argument("--ref-applies", type=int, default=10)
     ap.add_argument("--profile-fncb", type=int, default=0, metavar="NVEC",
                     help="only apply fncB three times to NVEC vectors (for ncu captures) and exit")
-    ap.add_argument("--profile-prec", choices=["c64", "c128"], default="c64")
+    ap.add_argument("--profile-prec", choices=["c64", "c128", "c128ds"], default="c64")
     ap.add_argument("--profile-tune", default=None, metavar="CHUNK,TPB[,LANES]",
                     help="with --profile-fncb: vectors per launch sequence, stencil threads per block and "
                          "threads per FFT pencil of the plane kernels (-1 default, 0 one)")

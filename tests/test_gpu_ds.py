@@ -111,3 +111,25 @@ def test_mixed_band_solve_with_ds_residuals(cuda, fame_lib):
         assert out[ds]["res"].max() <= 1e-8
     assert np.allclose(out[1]["ew"], out[0]["ew"], rtol=1e-10, atol=0)
     plan.close()
+
+
+def test_ds_lanes_and_autotune(cuda, fame_lib):
+    """Every compiled FFT split of the double-single plane kernels and both
+    stencil forms give the complex128 operator to 1e-13; the autotuner
+    times them and reports a compiled choice."""
+    import torch
+
+    n = 60
+    plan = fame.woodpile_plan(n, fame.band_path(npts=40)[[3, 17]])
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((2, 4 * n ** 3)) + 1j * rng.standard_normal((2, 4 * n ** 3))
+    xt = torch.from_numpy(x).cuda()
+    ref = plan.apply_B(xt).cpu().numpy()
+    for tpb in (0, 256):
+        for lanes in (-1, 3, 4, 5, 0):
+            plan.set_tune("c128ds", 2, 0, tpb, lanes)
+            got = _apply_ds(plan, xt).cpu().numpy()
+            assert relerr(got, ref) < 1e-13, (tpb, lanes, relerr(got, ref))
+    t = plan.autotune(nvec=2, prec="c128ds")
+    assert t["lanes"] in (-1, 3, 4, 5) and t["us"] > 0
+    plan.close()
