@@ -836,6 +836,8 @@ cudaError_t col(const PlanData<R>& d, cx<R>* w, int nfield, int nvec, long long 
 template <class R, int N>
 cudaError_t fncB_n(const Plan& P, const cx<R>* x, cx<R>* y, int nvec, const VecCtx& ctx, cx<R>* w0, cx<R>* w1,
                    cudaStream_t st, double2* pq, const cx<R>* pupd_z, const double* pupd_beta) {
+  static_assert(!std::is_same<R, ff>::value || plane_split(N) > 0,
+                "the double-single fncB reads and writes complex128 through the split plane kernels");
   PlanData<R> d = pdata<R>(P);
   if (!P.opt_pi_table) d.pi = nullptr;  // evaluate Pi in the plane kernels instead
   const long long Nq = P.Nq;
@@ -945,7 +947,10 @@ cudaError_t handle_n(const Plan& P, int which, const cx<R>* x, cx<R>* y, int nve
 
 // Grid sizes with a compiled double-single fncB (the residuals b - B x of the
 // mixed inner solves; other sizes take the FP64 fncB), and its declaration.
-#define FAME_FOR_EACH_DS_N(X) X(12) X(60)
+// (sizes with a split of the plane kernels: their loads and stores convert the
+// complex128 vectors; at n = 32 the unsplit double-single kernels were no
+// faster than FP64)
+#define FAME_FOR_EACH_DS_N(X) X(12) X(24) X(40) X(48) X(60)
 #define FAME_DS_SIGS(PFX, NN)                                                                                      \
   PFX cudaError_t fame::detail::fncB_n<fame::ff, NN>(const Plan&, const cx<fame::ff>*, cx<fame::ff>*, int,         \
                                                      const VecCtx&, cx<fame::ff>*, cx<fame::ff>*, cudaStream_t,    \

@@ -70,9 +70,9 @@ def band_structure(n=60, wave_vecs=None, bands=8, gamma=0.2, eps_in=13.0, width=
                 with lock:
                     t = tunes.get(len(idx))
                     if t is None:
-                        t = tunes[len(idx)] = plan.autotune(nvec=len(idx), prec="c64")
+                        tunes[len(idx)] = plan.autotune_mixed(nvec=len(idx))
                     else:
-                        plan.set_tune("c64", len(idx), t["chunk"], t["stencil_tpb"], t.get("lanes", -1))
+                        plan.set_tune_mixed(len(idx), t)
             r = plan.band_solve(bands, tol=tol, p=p, prec=prec, inner_tol=inner_tol, want_vectors=orgsep)
             if orgsep:
                 ev = r["ev"]

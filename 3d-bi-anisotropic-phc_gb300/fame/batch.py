@@ -60,7 +60,9 @@ def prepare_group(g, prec="c64", autotune=True, cache=None):
     alone on the GPU, before any concurrent work)."""
     t0 = time.perf_counter()
     plan = woodpile_plan(g["n"], g["kvecs"], gammas=g["gammas"])
-    tune = plan.autotune(prec=prec, cache=cache) if autotune else None
+    tune = None
+    if autotune:
+        tune = plan.autotune_mixed(cache=cache) if prec == "c64" else plan.autotune(prec=prec, cache=cache)
     torch.cuda.synchronize()
     return plan, tune, time.perf_counter() - t0
 

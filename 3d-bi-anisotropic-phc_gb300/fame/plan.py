@@ -265,6 +265,25 @@ class Plan:
             os.replace(tmp, cache)
         return dict(t, cached=False)
 
+    def autotune_mixed(self, nvec=None, cache=None):
+        """The launch parameters the mixed form uses: complex64 fncB (inner CG)
+        and, where the grid has it, the double-single fncB (the inner solves'
+        residuals).  Returns {'c64': ..., 'c128ds': ... or None}."""
+        out = {"c64": self.autotune(nvec=nvec, prec="c64", cache=cache), "c128ds": None}
+        try:
+            out["c128ds"] = self.autotune(nvec=nvec, prec="c128ds", cache=cache)
+        except L.FameError as e:
+            if e.code != L.FAME_ERR_UNSUPPORTED:
+                raise
+        return out
+
+    def set_tune_mixed(self, nvec, tunes):
+        """Installs what autotune_mixed returned (on another plan of the same
+        grid and batch width)."""
+        for prec, t in tunes.items():
+            if t:
+                self.set_tune(prec, nvec, t["chunk"], t["stencil_tpb"], t.get("lanes", -1))
+
     def set_tune(self, prec, nvec, chunk, stencil_tpb, lanes=-1):
         """fame_set_tune + fame_set_tune_lanes: install fncB launch parameters
         measured before (on another plan of the same grid, precision and

@@ -88,8 +88,8 @@ def test_ds_fncB_field_mode(cuda, fame_lib):
 def test_ds_unsupported_grid(cuda, fame_lib):
     import torch
 
-    plan = fame.woodpile_plan(8, [fame.fcc_point("X")])
-    x = torch.zeros(1, 4 * 8 ** 3, dtype=torch.complex128, device="cuda")
+    plan = fame.woodpile_plan(32, [fame.fcc_point("X")])
+    x = torch.zeros(1, 4 * 32 ** 3, dtype=torch.complex128, device="cuda")
     lib = fame.load()
     y = torch.empty_like(x)
     rc = lib.fame_apply_B(plan.raw, DS, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), 1, None, 0)
@@ -132,4 +132,20 @@ def test_ds_lanes_and_autotune(cuda, fame_lib):
             assert relerr(got, ref) < 1e-13, (tpb, lanes, relerr(got, ref))
     t = plan.autotune(nvec=2, prec="c128ds")
     assert t["lanes"] in (-1, 3, 4, 5) and t["us"] > 0
+    plan.close()
+
+
+@pytest.mark.parametrize("n", [24, 40, 48])
+def test_ds_fncB_other_grids(cuda, fame_lib, n):
+    """Every other grid with a compiled double-single fncB against the
+    complex128 operator."""
+    import torch
+
+    plan = fame.woodpile_plan(n, [fame.fcc_point("X"), fame.fcc_point("W")])
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((2, 4 * n ** 3)) + 1j * rng.standard_normal((2, 4 * n ** 3))
+    xt = torch.from_numpy(x).cuda()
+    ref = plan.apply_B(xt).cpu().numpy()
+    got = _apply_ds(plan, xt).cpu().numpy()
+    assert relerr(got, ref) < 1e-13, relerr(got, ref)
     plan.close()

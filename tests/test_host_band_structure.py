@@ -22,6 +22,13 @@ class FakePlan:
     def set_tune(self, prec, nvec, chunk, tpb, lanes=-1):
         self.tuned = ("set", nvec, chunk, tpb, lanes)
 
+    def autotune_mixed(self, nvec=None):
+        return {"c64": self.autotune(nvec=nvec, prec="c64"), "c128ds": self.autotune(nvec=nvec, prec="c128ds")}
+
+    def set_tune_mixed(self, nvec, tunes):
+        for prec, t in tunes.items():
+            self.set_tune(prec, nvec, t["chunk"], t["stencil_tpb"], t.get("lanes", -1))
+
     def band_solve(self, k, tol, p, prec, inner_tol, want_vectors):
         key = self.kv[:, 0][:, None]  # first wave-vector component identifies the k-point
         om = key + np.arange(k)[None, :] / 100.0
