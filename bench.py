@@ -60,10 +60,11 @@ INNER_TOL_MIXED = 3e-12    # B^{-1} of the mixed form (complex64 CG + FP64 resid
 # (Computational_settings_Lanczos.m:30), which the plain FP64 sample keeps.
 # More columns cut the restarts at the batches holding Gamma, whose two
 # shifted zero modes occupy part of the Krylov space: 2k + 4 gave +23 % over
-# the path at n = 60 (residuals <= 4e-9), 2k + 6 another +3 % (residuals
-# <= 5.2e-9); 2k + 8 adds 1.4 % more with residuals up to 7.4e-9, too close
-# to the 1e-8 bar.
-LANCZOS_P_MIXED = 2 * BANDS + 6
+# the path at n = 60, 2k + 6 another +3 %.  With the inner tolerance 3e-12
+# (relaxed) and the double-single residuals: 2k + 6 -> 2.624 k-point solves/s
+# (worst residual 2.95e-9), 2k + 8 -> 2.675 (3.22e-9), 2k + 10 -> 2.687
+# (2.60e-9), 2k + 12 -> 2.680 (3.08e-9).
+LANCZOS_P_MIXED = 2 * BANDS + 10
 RES_TOL = 1e-8
 PATH_POINTS = 40
 # The FP64 oracle's own Lanczos.m solve of the woodpile at n = 60, X point
