@@ -114,7 +114,7 @@ struct Plan {
   int opt_precond = 1;                // CG on B preconditioned by the averaged-medium B0^{-1}
   double opt_tol32 = 1e-6;            // complex64 CG tolerance of the first refinement round
   int opt_ds_residual = 1;            // mixed B^{-1}: residuals through the double-single fncB
-  double opt_relax = 0.5;             // mixed Lanczos: relax the inner tolerance once Ritz residuals < this
+  double opt_relax = 0.9;             // mixed Lanczos: relax the inner tolerance once Ritz residuals < this
   double opt_relax_max = 1e6;         // largest relaxation factor
   int opt_c64_round = 1;              // mixed B^{-1}: second round's B x update in complex64 (0: FP64 apply)
   int opt_graph = 2;                  // CG from CUDA graphs: 1 blocks of iterations, 2 the whole loop

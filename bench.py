@@ -445,7 +445,7 @@ def run_fame(args):
                            fncb_tune_c128ds={k: int(tuneds[k]) for k in ("chunk", "stencil_tpb", "lanes")},
                            precision="complex64 fncB + preconditioned CG, FP64 recurrence/reorth, residual "
                                      f"refinement with the double-single fncB (B^-1 to {INNER_TOL_MIXED:g}, tighter near Gamma, relaxed by "
-                                     "0.5 / (largest relative Ritz residual) for later Lanczos vectors), FP64 "
+                                     "0.9 / (largest relative Ritz residual) for later Lanczos vectors), FP64 "
                                      "Rayleigh-Ritz refinement sweep of every Ritz pair, FP64 NFSEP check",
                            l2="inputs larger than L2 (Lanczos basis and B*Q of a batch "
                               f"{2 * args.batch * args.lanczos_p * 4 * N_GRID ** 3 * 16 / 1e9:.1f} GB)"),

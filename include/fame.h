@@ -122,7 +122,7 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *                     B x with a complex64 apply of its correction [1]
  *                     (estimates the residual to ~1e-11 of b); 0 takes an
  *                     FP64 apply in every round (B x exact after each).
- *   FAME_OPT_RELAX    mixed Lanczos: c in [0, 1) [0.5; 0 = off].  At a
+ *   FAME_OPT_RELAX    mixed Lanczos: c in [0, 1) [0.9; 0 = off].  At a
  *                     restart where every wanted Ritz pair's relative
  *                     residual r is below c, the instance's inner tolerance is
  *                     multiplied by min(FAME_OPT_RELAX_MAX, c / max r) (relaxed inner
