@@ -290,8 +290,8 @@ int minres_shifted(Plan& P, const cx<R>* b, cx<R>* x, const int* d_inst, double 
       FAME_KERNELS_RAN(body_nodes * (unsigned long long)np);
       done_steps = np * kMinresBlock;
       if (hst.nan) return fail(&P, FAME_ERR_NAN, "minres: non-finite value");
-    } else if (ge != cudaErrorNotSupported) {
-      JD_CK(ge, "minres graph loop");
+    } else {
+      cudaGetLastError();  // no graph loop (nothing of it ran): the blocks below take over
     }
   }
   while (done_steps < maxit && hst.active) {

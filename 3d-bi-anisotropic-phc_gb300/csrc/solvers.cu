@@ -235,8 +235,8 @@ int pcg_batched(Plan& P, const cx<R>* b, cx<R>* x, int nvec, const int* d_inst, 
       FAME_KERNELS_RAN(body_nodes * (unsigned long long)passes);
       it = 1 + passes * chk;
       any = std::any_of(act.begin(), act.end(), [](int a) { return a != 0; });
-    } else if (ge != cudaErrorNotSupported) {
-      FAME_CK(ge, "pcg graph loop");
+    } else {
+      cudaGetLastError();  // no graph loop (nothing of it ran): the blocks below take over
     }
   }
   for (; it <= maxit && any; it += chk) {
