@@ -632,13 +632,15 @@ def main():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=10,
-                    help="k-points per step (batched band solve); 10 = the 40-point path in four steps, whose "
-                         "fncB runs as two sub-batches of 5 vectors (fills the last wave of plane-kernel CTAs)")
+                    help="k-points per batched band solve (a step solves --concurrent of them); 10 = the "
+                         "40-point path in four batches, whose fncB runs as two sub-batches of 5 vectors "
+                         "(fills the last wave of plane-kernel CTAs)")
     ap.add_argument("--impl", choices=["fame", "reference"], default="fame")
     ap.add_argument("--concurrent", type=int, default=2,
                     help="batches solved at once per step, each on its own stream and host thread "
-                         "(2: the four path batches in two steps; measured at n = 60: 1 -> 1.90, "
-                         "2 -> 2.12, 3 -> 2.20, 4 -> 2.19 k-point solves/s, GPU busy 97.6 -> 99.5 %%)")
+                         "(2: the four path batches in two steps; measured at n = 60 before the relaxed "
+                         "inner tolerance: 1 -> 1.90, 2 -> 2.12, 3 -> 2.20, 4 -> 2.19 k-point solves/s, "
+                         "GPU busy 97.6 -> 99.5 %%)")
     ap.add_argument("--lanczos-tol", type=float, default=LANCZOS_TOL_MIXED,
                     help="Lanczos tolerance of the mixed form (the FP64 form keeps the reference's 1e-10)")
     ap.add_argument("--lanczos-p", type=int, default=LANCZOS_P_MIXED,
