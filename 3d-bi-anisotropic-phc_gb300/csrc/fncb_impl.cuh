@@ -430,7 +430,7 @@ template <int G, class F> __device__ __forceinline__ void with_g(int g, F&& f) {
   });
 }
 
-template <class R, int N, int G>
+template <class R, int N, int G, bool UPD>
 __global__ void __launch_bounds__(Split<N, G>::TB, plane_min_blocks<R, N, G>())
 k_plane_inv2(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d, VecCtx ctx,
              long long in_stride, long long in_side_stride, long long out_stride, int side0, DirUpd<R> upd) {
@@ -460,7 +460,7 @@ k_plane_inv2(const cx<R>* __restrict__ x, cx<R>* __restrict__ out, PlanData<R> d
         in[it][1] = load_io<R>(xin + Nq + e);
       }
     }
-    if (upd.z) {  // p = z + beta p, written back
+    if constexpr (UPD) {  // p = z + beta p, written back (UPD: upd.z set)
       const long long off = vec * in_stride + blockIdx.y * in_side_stride + (long long)k3 * N * N;
       const cx<R>* zin = upd.z + off;
       cx<R>* xw = const_cast<cx<R>*>(x) + off;
@@ -693,15 +693,22 @@ cudaError_t plane_inv(const Plan& P, const PlanData<R>& d, const cx<R>* x, cx<R>
     const int lanes = plane_lanes<R, N>(P, tuned_lanes);
     if (lanes > 0) {
       cudaError_t e = cudaErrorInvalidValue;
-      with_lanes<R, N>(lanes, [&](auto gc) {
-        constexpr int G = decltype(gc)::value;
-        auto kfn = k_plane_inv2<R, N, G>;
+      // the CG direction update is compiled into its own variant, so the
+      // plain operator carries none of its code (the double-single operator
+      // never takes it)
+      auto launch = [&](auto kfn, int tb) {
         e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return;
         FAME_LAUNCHED(1);
-        kfn<<<dim3(N, nside, nvec), Split<N, G>::TB, sm, st>>>(x, out, d, ctx, in_stride, in_side_stride,
-                                                               out_stride, side0, upd);
+        kfn<<<dim3(N, nside, nvec), tb, sm, st>>>(x, out, d, ctx, in_stride, in_side_stride, out_stride, side0, upd);
         e = cudaGetLastError();
+      };
+      with_lanes<R, N>(lanes, [&](auto gc) {
+        constexpr int G = decltype(gc)::value;
+        if constexpr (!std::is_same<R, ff>::value) {
+          if (upd.z) return launch(k_plane_inv2<R, N, G, true>, Split<N, G>::TB);
+        }
+        launch(k_plane_inv2<R, N, G, false>, Split<N, G>::TB);
       });
       return e;
     }
