@@ -116,7 +116,7 @@ struct Plan {
   int opt_ds_residual = 1;            // mixed B^{-1}: residuals through the double-single fncB
   double opt_relax = 0.9;             // mixed Lanczos: relax the inner tolerance once Ritz residuals < this
   double opt_relax_max = 1e6;         // largest relaxation factor
-  int opt_c64_round = 1;              // mixed B^{-1}: second round's B x update in complex64 (0: FP64 apply)
+  int opt_c64_round = 1;              // mixed B^{-1}: second round's B x update in complex64 (0: exact apply)
   int opt_graph = 2;                  // CG from CUDA graphs: 1 blocks of iterations, 2 the whole loop
   double opt_itol_floor = 1e-13;      // mixed form: floor of the spread-scaled inner tolerance
   int opt_plane_split = 1;            // fncB plane kernels with several threads per pencil where compiled

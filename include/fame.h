@@ -120,8 +120,9 @@ int fame_set_stream(fame_plan_t plan, void* stream);
  *                     (same values to rounding).  Complex64 always evaluates.
  *   FAME_OPT_C64_ROUND  mixed B^{-1}: the second refinement round updates
  *                     B x with a complex64 apply of its correction [1]
- *                     (estimates the residual to ~1e-11 of b); 0 takes an
- *                     FP64 apply in every round (B x exact after each).
+ *                     (estimates the residual to ~1e-11 of b); 0 takes the
+ *                     exact apply (double-single or FP64, see
+ *                     FAME_OPT_DS_RESIDUAL) in every round.
  *   FAME_OPT_RELAX    mixed Lanczos: c in [0, 1) [0.9; 0 = off].  At a
  *                     restart where every wanted Ritz pair's relative
  *                     residual r is below c, the instance's inner tolerance is
